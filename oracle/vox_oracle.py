@@ -1,0 +1,204 @@
+"""ctypes wrapper of the CPU oracle (liboracle_vox.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline legs as the checker. Parity status: unpinned (see vox_oracle.h).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle_vox.so")
+
+_LIB = None
+_P = ctypes.c_void_p
+
+
+class _Coord(ctypes.Structure):
+    _fields_ = [("x", ctypes.c_int32), ("y", ctypes.c_int32), ("z", ctypes.c_int32)]
+
+
+def load() -> ctypes.CDLL:
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        import sys
+        sys.path.insert(0, os.path.join(os.path.dirname(HERE), "wgpu-voxel-engine_gb300"))
+        from voxgpu import _build  # noqa: E402
+        _build.build_oracle()
+    L = ctypes.CDLL(LIB_PATH)
+    sig = {
+        "or_splitmix64_next": (ctypes.c_uint64, [ctypes.POINTER(ctypes.c_uint64)]),
+        "or_perm_init": (None, [ctypes.c_uint64, _P]),
+        "or_noise2_f32": (ctypes.c_float, [_P, ctypes.c_float, ctypes.c_float]),
+        "or_noise3_f32": (ctypes.c_float, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float]),
+        "or_noise2_f64": (ctypes.c_double, [_P, ctypes.c_double, ctypes.c_double]),
+        "or_noise3_f64": (ctypes.c_double, [_P, ctypes.c_double, ctypes.c_double,
+                                            ctypes.c_double]),
+        "or_generate_cubes": (ctypes.c_int, [_P, _Coord, ctypes.c_int64, _P]),
+        "or_cubes_to_occ": (None, [ctypes.c_int, _P, _P]),
+        "or_occ_to_cubes": (None, [ctypes.c_int, _P, _P]),
+        "or_cull_faces": (ctypes.c_int64, [ctypes.c_int, ctypes.c_int, _P, _P, _P,
+                                           ctypes.c_int64]),
+        "or_face_rotation": (None, [ctypes.c_int, _P]),
+        "or_instance_raw": (None, [ctypes.c_int, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                   ctypes.c_uint32, _P]),
+        "or_face_vertices": (None, [ctypes.c_int, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                    ctypes.c_uint32, _P, _P]),
+        "or_dir_slot": (ctypes.c_int, [ctypes.c_int]),
+        "or_mesh_chunk": (ctypes.c_int64, [_P, _Coord, _P, _P, _P, _P, ctypes.c_int64]),
+        "or_gen_mesh_batch": (ctypes.c_int64, [_P, _P, _P, ctypes.c_int32, ctypes.c_int64, _P, _P,
+                                               ctypes.c_int64, _P]),
+        "or_baseline_run": (ctypes.c_int64, [_P, _P, _P, ctypes.c_int32, ctypes.c_int64,
+                                             ctypes.c_int]),
+        "or_frustum_planes": (None, [_P, _P]),
+        "or_frustum_contains": (ctypes.c_int, [_P, _Coord, ctypes.c_int]),
+        "or_noise_error_stats": (ctypes.c_int, [_P, _P, ctypes.c_int32,
+                                                ctypes.POINTER(ctypes.c_double),
+                                                ctypes.POINTER(ctypes.c_int64),
+                                                ctypes.POINTER(ctypes.c_int64)]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _LIB = L
+    return L
+
+
+def _addr(a) -> int:
+    return 0 if a is None else int(a.ctypes.data)
+
+
+def _cfg_addr(cfg) -> int:
+    return ctypes.addressof(cfg)
+
+
+def coords_array(coords) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(coords, dtype=np.int32).reshape(-1, 3))
+
+
+def perm(seed: int) -> np.ndarray:
+    p = np.zeros(512, np.uint8)
+    load().or_perm_init(seed, _addr(p))
+    return p
+
+
+def generate_cubes(cfg, coord, chunk_index: int = 0) -> np.ndarray:
+    n = cfg.chunk_size
+    out = np.zeros(n * n * n, np.uint8)
+    st = load().or_generate_cubes(_cfg_addr(cfg), _Coord(*coord), chunk_index, _addr(out))
+    assert st == 0, st
+    return out
+
+
+def cubes_to_occ(n: int, cubes: np.ndarray) -> np.ndarray:
+    w = n // 32 if n > 32 else 1
+    occ = np.zeros(n * n * w, np.uint32)
+    load().or_cubes_to_occ(n, _addr(np.ascontiguousarray(cubes, np.uint8)), _addr(occ))
+    return occ
+
+
+def occ_to_cubes(n: int, occ: np.ndarray) -> np.ndarray:
+    cubes = np.zeros(n * n * n, np.uint8)
+    load().or_occ_to_cubes(n, _addr(np.ascontiguousarray(occ, np.uint32)), _addr(cubes))
+    return cubes
+
+
+def _adj_array(adj):
+    adj = list(adj or []) + [None] * 6
+    keep = [None if a is None else np.ascontiguousarray(a, np.uint8) for a in adj[:6]]
+    arr = (_P * 6)(*[_P(_addr(a)) for a in keep])
+    return arr, keep
+
+
+def cull_faces(n: int, cull_mode: int, cubes: np.ndarray, adj=None) -> np.ndarray:
+    """Faces as an (F, 4) uint8 array of (x, y, z, dir) in emission order."""
+    arr, keep = _adj_array(adj)
+    cubes = np.ascontiguousarray(cubes, np.uint8)
+    L = load()
+    cnt = L.or_cull_faces(n, cull_mode, _addr(cubes), ctypes.addressof(arr), None, 0)
+    out = np.zeros((max(cnt, 1), 4), np.uint8)
+    L.or_cull_faces(n, cull_mode, _addr(cubes), ctypes.addressof(arr), _addr(out), cnt)
+    del keep
+    return out[:cnt]
+
+
+def face_rotation(d: int) -> np.ndarray:
+    r = np.zeros((3, 3), np.float32)
+    load().or_face_rotation(d, _addr(r))
+    return r
+
+
+def bytes_per_face(layout: int):
+    return (68, 0) if layout == 1 else (96, 24)
+
+
+def mesh_chunk(cfg, coord, cubes, adj=None):
+    """Returns (out0 bytes, out1 bytes, face count) of one chunk."""
+    arr, keep = _adj_array(adj)
+    cubes = np.ascontiguousarray(cubes, np.uint8)
+    L = load()
+    cnt = L.or_mesh_chunk(_cfg_addr(cfg), _Coord(*coord), _addr(cubes), ctypes.addressof(arr),
+                          None, None, 0)
+    b0, b1 = bytes_per_face(cfg.layout)
+    o0 = np.zeros(max(cnt, 1) * b0, np.uint8)
+    o1 = np.zeros(max(cnt, 1) * max(b1, 1), np.uint8)
+    L.or_mesh_chunk(_cfg_addr(cfg), _Coord(*coord), _addr(cubes), ctypes.addressof(arr),
+                    _addr(o0), _addr(o1), cnt)
+    del keep
+    return o0[:cnt * b0], o1[:cnt * b1], cnt
+
+
+def gen_mesh_batch(cfg, coords, masks=None, index_base: int = 0, cap: int | None = None):
+    """Oracle of vox_gen_mesh_batch: (out0 bytes, out1 bytes, offsets[n+1])."""
+    c = coords_array(coords)
+    n = len(c)
+    m = None if masks is None else np.ascontiguousarray(np.asarray(masks, np.uint8))
+    L = load()
+    offs = np.zeros(n + 1, np.uint64)
+    total = L.or_gen_mesh_batch(_cfg_addr(cfg), _addr(c), _addr(m), n, index_base, None, None, 0,
+                                _addr(offs))
+    if cap is None:
+        cap = total
+    b0, b1 = bytes_per_face(cfg.layout)
+    o0 = np.zeros(max(cap, 1) * b0, np.uint8)
+    o1 = np.zeros(max(cap, 1) * max(b1, 1), np.uint8)
+    L.or_gen_mesh_batch(_cfg_addr(cfg), _addr(c), _addr(m), n, index_base, _addr(o0), _addr(o1),
+                        cap, _addr(offs))
+    w = min(total, cap)
+    return o0[:w * b0], o1[:w * b1], offs
+
+
+def baseline_run(cfg, coords, masks, index_base: int, nthreads: int) -> int:
+    c = coords_array(coords)
+    m = None if masks is None else np.ascontiguousarray(np.asarray(masks, np.uint8))
+    return int(load().or_baseline_run(_cfg_addr(cfg), _addr(c), _addr(m), len(c), index_base,
+                                      nthreads))
+
+
+def frustum_planes(m_colmajor) -> np.ndarray:
+    m = np.ascontiguousarray(np.asarray(m_colmajor, np.float32).reshape(16))
+    out = np.zeros(24, np.float32)
+    load().or_frustum_planes(_addr(m), _addr(out))
+    return out
+
+
+def frustum_contains(planes, coord, extent: int) -> bool:
+    p = np.ascontiguousarray(np.asarray(planes, np.float32).reshape(24))
+    return bool(load().or_frustum_contains(_addr(p), _Coord(*coord), extent))
+
+
+def noise_error_stats(cfg, coords):
+    c = coords_array(coords)
+    err = ctypes.c_double()
+    near = ctypes.c_int64()
+    mism = ctypes.c_int64()
+    st = load().or_noise_error_stats(_cfg_addr(cfg), _addr(c), len(c), ctypes.byref(err),
+                                     ctypes.byref(near), ctypes.byref(mism))
+    assert st == 0, st
+    return err.value, near.value, mism.value

@@ -1,0 +1,75 @@
+"""The C ABI without a GPU: the library builds, loads and exports every entry point that
+include/voxgpu.h declares; argument validation that needs no device works; and calls
+that do need a device fail loudly instead of falling back to the CPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for h in sorted(os.listdir(os.path.join(REPO, "include"))):
+        if not h.endswith(".h"):
+            continue
+        text = open(os.path.join(REPO, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"^[A-Za-z_][\w \*]*?\b(vox_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for required in ("vox_ctx_create", "vox_generate", "vox_mesh", "vox_mesh_batch",
+                     "vox_gen_mesh_batch", "vox_gen_mesh_host", "vox_frustum_cull"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(vox):
+    lib = vox.lib()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_abi_version_and_sizes(vox):
+    assert vox.lib().vox_abi_version() == 1
+    cfg = vox.make_config(chunk_size=32)
+    s = vox.query_sizes(cfg)
+    assert s.occ_words_per_chunk == 32 * 32
+    assert (s.bytes_per_face_out0, s.bytes_per_face_out1) == (96, 24)
+    cfg = vox.make_config(chunk_size=64, layout=vox.LAYOUT_INSTANCED)
+    s = vox.query_sizes(cfg)
+    assert s.occ_words_per_chunk == 64 * 64 * 2
+    assert (s.bytes_per_face_out0, s.bytes_per_face_out1) == (68, 0)
+    # C layout of vox_config: 3 ints, 6 u32, pad to 8, then vox_generator (48 bytes).
+    assert ctypes.sizeof(vox.Generator) == 48
+    assert vox.Config.gen.offset == 40 and ctypes.sizeof(vox.Config) == 88
+    assert ctypes.sizeof(vox.ChunkCoord) == 12
+
+
+@pytest.mark.parametrize("field,value", [("chunk_size", 12), ("chunk_size", 128),
+                                         ("layout", 7), ("cull_mode", 3)])
+def test_invalid_config_rejected(vox, field, value):
+    cfg = vox.make_config()
+    setattr(cfg, field, value)
+    s = vox.Sizes()
+    assert vox.lib().vox_query_sizes(ctypes.byref(cfg), ctypes.byref(s)) == vox.VOX_ERR_INVALID
+
+
+def test_frustum_planes_host_function(vox, oracle):
+    import numpy as np
+    rng = np.random.default_rng(5)
+    m = rng.standard_normal(16).astype(np.float32)
+    assert np.array_equal(np.array(vox.frustum_planes(m), np.float32), oracle.frustum_planes(m))
+
+
+def test_no_cpu_fallback_without_gpu(vox):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible; covered by the gpu tests")
+    with pytest.raises(vox.VoxError) as e:
+        vox.Context(vox.make_config())
+    assert e.value.status in (vox.VOX_ERR_NO_DEVICE, vox.VOX_ERR_CUDA)

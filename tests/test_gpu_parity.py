@@ -1,0 +1,318 @@
+"""Parity of the CUDA path with the CPU oracle, through the C ABI (bit-exact).
+
+Occupancy, face counts, offsets and every byte of the emitted vertex / index /
+instance records must equal the oracle's on the same inputs (signed zeros included).
+"""
+import numpy as np
+import pytest
+
+from gpu_util import ctx_for, dev_bytes, gpu_gen_mesh, gpu_generate, to_dev, to_np
+
+pytestmark = pytest.mark.gpu
+
+LAYOUTS = [0, 1]  # vertex, instanced
+
+
+def small_coords():
+    return [(0, 0, 0), (-1, 0, 0), (2, -1, 3), (-3, 1, -2), (5, 0, -7), (0, 2, 1)]
+
+
+def gen_cfg(vox, kind, n, layout=0, cull=0):
+    if kind == "height":
+        return vox.make_config(chunk_size=n, layout=layout, cull_mode=cull, kind=vox.GEN_HEIGHTMAP,
+                               octaves=4, seed=7, frequency=1 / 128, amplitude=48.0,
+                               base_height=float(n // 2))
+    if kind == "height1":
+        return vox.make_config(chunk_size=n, layout=layout, cull_mode=cull, kind=vox.GEN_HEIGHTMAP,
+                               octaves=1, seed=42, frequency=1 / 64, amplitude=12.0,
+                               base_height=4.0)
+    if kind == "density":
+        return vox.make_config(chunk_size=n, layout=layout, cull_mode=cull, kind=vox.GEN_DENSITY,
+                               octaves=3, seed=1234, frequency=1 / 96, y_ref=float(n // 2),
+                               y_scale=1 / 64)
+    if kind == "refdensity":  # the reference's parameters and fill rule (noise < 0 -> solid)
+        return vox.make_config(chunk_size=n, layout=layout, cull_mode=cull, kind=vox.GEN_DENSITY,
+                               octaves=3, seed=1, frequency=0.09, lacunarity=0.5, gain=2.5,
+                               solid_below_zero=1)
+    return vox.make_config(chunk_size=n, layout=layout, cull_mode=cull, kind=vox.GEN_BERNOULLI,
+                           seed=99)
+
+
+@pytest.mark.parametrize("n", [8, 16, 32, 64])
+@pytest.mark.parametrize("kind", ["height", "height1", "density", "refdensity", "bernoulli"])
+def test_generate_matches_oracle(vox, oracle, n, kind):
+    cfg = gen_cfg(vox, kind, n)
+    coords = small_coords()
+    got = gpu_generate(vox, cfg, coords, index_base=11)
+    for i, c in enumerate(coords):
+        want = oracle.cubes_to_occ(n, oracle.generate_cubes(cfg, c, 11 + i))
+        assert np.array_equal(got[i], want), (kind, n, c)
+
+
+@pytest.mark.parametrize("n", [8, 16, 32, 64])
+def test_cubes_occ_roundtrip(vox, oracle, n):
+    rng = np.random.default_rng(n)
+    cfg = vox.make_config(chunk_size=n)
+    k = 3
+    cubes = rng.choice(np.array([0, 1, 2], np.uint8), size=k * n ** 3, p=[0.4, 0.1, 0.5])
+    ctx = ctx_for(vox, cfg)
+    words = ctx.sizes.occ_words_per_chunk
+    d_c = to_dev(cubes)
+    d_o = dev_bytes(k * words * 4)
+    ctx.cubes_to_occ(d_c, k, d_o)
+    occ = to_np(d_o, k * words * 4).view(np.uint32).reshape(k, words)
+    for i in range(k):
+        assert np.array_equal(occ[i], oracle.cubes_to_occ(n, cubes[i * n ** 3:(i + 1) * n ** 3]))
+    d_back = dev_bytes(k * n ** 3)
+    ctx.occ_to_cubes(d_o, k, d_back)
+    back = to_np(d_back, k * n ** 3)
+    assert np.array_equal(back, np.where(cubes == 2, 2, 0).astype(np.uint8))
+
+
+def patterns(n, rng):
+    """Occupancy patterns of the known-answer tests plus random densities."""
+    idx = np.arange(n ** 3)
+    x, z, y = idx % n, (idx // n) % n, idx // (n * n)
+    out = {
+        "air": np.full(n ** 3, 2, np.uint8),
+        "solid": np.zeros(n ** 3, np.uint8),
+        "checker": np.where((x + y + z) % 2 == 0, 0, 2).astype(np.uint8),
+        "one": np.where((x == 3) & (y == 2) & (z == n - 1), 0, 2).astype(np.uint8),
+    }
+    for p in (0.1, 0.5, 0.9):
+        out[f"rand{p}"] = np.where(rng.random(n ** 3) < p, 0, 2).astype(np.uint8)
+    return out
+
+
+def run_mesh_single(vox, cfg, cubes, adj, coord):
+    n = cfg.chunk_size
+    ctx = ctx_for(vox, cfg)
+    occ = oracle_occ = None
+    import vox_oracle
+    oracle_occ = vox_oracle.cubes_to_occ(n, cubes)
+    occ = to_dev(oracle_occ)
+    nb = [None if a is None else to_dev(vox_oracle.cubes_to_occ(n, a)) for a in adj]
+    cap = ctx.sizes.max_faces_per_chunk
+    b0, b1 = ctx.sizes.bytes_per_face_out0, ctx.sizes.bytes_per_face_out1
+    o0 = dev_bytes(cap * b0, 0xEE)
+    o1 = dev_bytes(cap * b1, 0xEE)
+    cnt = to_dev(np.zeros(1, np.uint64))
+    ctx.mesh(occ, nb, coord, o0, o1 if b1 else None, cap, cnt)
+    ctx.sync()
+    c = int(to_np(cnt)[0])
+    r = to_np(o0, c * b0), (to_np(o1, c * b1) if b1 else np.zeros(0, np.uint8)), c
+    ctx.close()
+    return r
+
+
+@pytest.mark.parametrize("n", [8, 16, 32, 64])
+@pytest.mark.parametrize("layout", LAYOUTS)
+@pytest.mark.parametrize("cull", [0, 1])
+def test_mesh_single_matches_oracle(vox, oracle, n, layout, cull):
+    rng = np.random.default_rng(100 * n + 10 * layout + cull)
+    cfg = vox.make_config(chunk_size=n, layout=layout, cull_mode=cull)
+    pats = patterns(n, rng)
+    names = list(pats)
+    for k, name in enumerate(names):
+        cubes = pats[name]
+        adj = []
+        for d in range(6):
+            choice = rng.integers(0, 3)
+            adj.append(None if choice == 0 else pats[names[rng.integers(0, len(names))]])
+        coord = (int(rng.integers(-50, 50)), int(rng.integers(-5, 5)), int(rng.integers(-50, 50)))
+        w0, w1, wc = oracle.mesh_chunk(cfg, coord, cubes, adj)
+        g0, g1, gc = run_mesh_single(vox, cfg, cubes, adj, coord)
+        assert gc == wc, (name, gc, wc)
+        assert np.array_equal(g0, w0), name
+        assert np.array_equal(g1, w1), name
+
+
+@pytest.mark.parametrize("n", [16, 32])
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_mesh_batch_pool_matches_oracle(vox, oracle, n, layout):
+    rng = np.random.default_rng(7 + n + layout)
+    cfg = vox.make_config(chunk_size=n, layout=layout)
+    slots = 9
+    pool_cubes = [np.where(rng.random(n ** 3) < p, 0, 2).astype(np.uint8)
+                  for p in rng.uniform(0.05, 0.95, slots)]
+    pool = np.concatenate([oracle.cubes_to_occ(n, c) for c in pool_cubes])
+    m = 14
+    sl = rng.integers(0, slots, m).astype(np.int32)
+    nbr = rng.integers(-1, slots, (m, 6)).astype(np.int32)
+    coords = [(int(a), 0, int(b)) for a, b in rng.integers(-20, 20, (m, 2))]
+    ctx = ctx_for(vox, cfg)
+    b0, b1 = ctx.sizes.bytes_per_face_out0, ctx.sizes.bytes_per_face_out1
+    cap = ctx.sizes.max_faces_per_chunk * m
+    o0, o1 = dev_bytes(cap * b0), dev_bytes(cap * b1)
+    offs = to_dev(np.zeros(m + 1, np.uint64))
+    ctx.mesh_batch(to_dev(pool), slots, to_dev(sl), to_dev(nbr), to_dev(np.array(coords, np.int32)),
+                   m, o0, o1 if b1 else None, cap, offs)
+    ctx.sync()
+    offsets = to_np(offs)
+    total = int(offsets[m])
+    g0 = to_np(o0, total * b0)
+    g1 = to_np(o1, total * b1) if b1 else None
+    acc = 0
+    for i in range(m):
+        adj = [None if nbr[i, d] < 0 else pool_cubes[nbr[i, d]] for d in range(6)]
+        w0, w1, wc = oracle.mesh_chunk(cfg, coords[i], pool_cubes[sl[i]], adj)
+        assert int(offsets[i]) == acc
+        assert np.array_equal(g0[acc * b0:(acc + wc) * b0], w0)
+        if b1:
+            assert np.array_equal(g1[acc * b1:(acc + wc) * b1], w1)
+        acc += wc
+    assert acc == total
+    ctx.close()
+
+
+def compare_batch(vox, oracle, cfg, coords, masks, index_base=0):
+    w0, w1, woffs = oracle.gen_mesh_batch(cfg, coords, masks, index_base)
+    total = int(woffs[-1])
+    g0, g1, goffs, _ = gpu_gen_mesh(vox, cfg, coords, masks, index_base, cap=max(total, 1))
+    assert np.array_equal(goffs, woffs)
+    assert np.array_equal(g0, w0)
+    assert np.array_equal(g1, w1)
+    return total
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_plain_workload_full(vox, oracle, layout):
+    """8x8 chunks of 32^3 around the origin, 2-D Perlin heightmap (the CPU-runnable case)."""
+    wl = vox.workload("plain")
+    total = compare_batch(vox, oracle, wl.config(layout=layout), wl.coords, wl.masks())
+    assert total > 0
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_heightmap_workload_full(vox, oracle, layout):
+    """32x32 chunks of 16^3, 2-D fBm: all-air, all-solid and surface chunks."""
+    wl = vox.workload("heightmap")
+    total = compare_batch(vox, oracle, wl.config(layout=layout), wl.coords, wl.masks())
+    assert total > 0
+
+
+@pytest.mark.parametrize("cull", [0, 1])
+def test_density_workload_slab(vox, oracle, cull):
+    """A 4x3x4 block of the 3-D density terrain around its surface (y = 256)."""
+    wl = vox.workload("density")
+    coords = vox.grid_coords(range(4, 8), range(7, 10), range(4, 8))
+    total = compare_batch(vox, oracle, wl.config(cull_mode=cull), coords,
+                          vox.neighbour_masks(coords, full6=bool(cull)))
+    assert total > 0
+
+
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_stress_workload_sample(vox, oracle, layout):
+    """Four isolated 64^3 Bernoulli(0.5) chunks (index base 1000)."""
+    wl = vox.workload("stress")
+    coords = [(i, 0, 0) for i in range(4)]
+    total = compare_batch(vox, oracle, wl.config(layout=layout), coords, None, index_base=1000)
+    assert total > 4 * 300_000
+
+
+def test_capacity_overflow_reports_and_keeps_prefix(vox, oracle):
+    wl = vox.workload("heightmap")
+    cfg = wl.config()
+    coords = wl.coords[:64]
+    masks = vox.neighbour_masks(coords)
+    w0, w1, woffs = oracle.gen_mesh_batch(cfg, coords, masks)
+    total = int(woffs[-1])
+    cap = total // 3
+    g0, g1, goffs, st = gpu_gen_mesh(vox, cfg, coords, masks, cap=cap, expect_status=True)
+    assert st == vox.VOX_ERR_CAPACITY
+    assert np.array_equal(goffs, woffs)
+    assert np.array_equal(g0, w0[:cap * 96]) and np.array_equal(g1, w1[:cap * 24])
+
+
+def test_chunk_bytes_independent_of_batch(vox, oracle):
+    """A chunk's mesh is the same alone and inside any batch (indices are chunk-local)."""
+    wl = vox.workload("plain")
+    cfg = wl.config()
+    coords = list(wl.coords)
+    masks = wl.masks()
+    a0, a1, aoffs, _ = gpu_gen_mesh(vox, cfg, coords, masks, cap=2_000_000)
+    for k in (0, 17, 63):
+        s0, s1, soffs, _ = gpu_gen_mesh(vox, cfg, [coords[k]], [masks[k]], cap=200_000)
+        lo, hi = int(aoffs[k]), int(aoffs[k + 1])
+        assert hi - lo == int(soffs[1])
+        assert np.array_equal(a0[lo * 96:hi * 96], s0)
+        assert np.array_equal(a1[lo * 24:hi * 24], s1)
+
+
+def test_repeat_launches_identical(vox):
+    """Back-to-back launches on one context (epoch-tagged look-back) give the same bytes."""
+    wl = vox.workload("heightmap")
+    cfg = wl.config()
+    ctx = ctx_for(vox, cfg)
+    n = len(wl.coords)
+    d_coords = to_dev(np.asarray(wl.coords, np.int32))
+    d_mask = to_dev(np.asarray(wl.masks(), np.uint8))
+    cap = 3_000_000
+    o0, o1 = dev_bytes(cap * 96), dev_bytes(cap * 24)
+    offs = to_dev(np.zeros(n + 1, np.uint64))
+    digests = []
+    for _ in range(5):
+        ctx.gen_mesh_batch(d_coords, d_mask, n, o0, o1, cap, offs)
+        ctx.sync()
+        total = int(to_np(offs)[n])
+        digests.append((total, hash(to_np(o0, total * 96).tobytes()),
+                        hash(to_np(o1, total * 24).tobytes())))
+    assert len(set(digests)) == 1
+    ctx.close()
+
+
+def test_host_entry_point_matches_oracle(vox, oracle):
+    wl = vox.workload("plain")
+    cfg = wl.config()
+    coords = np.asarray(wl.coords, np.int32)
+    masks = np.asarray(wl.masks(), np.uint8)
+    w0, w1, woffs = oracle.gen_mesh_batch(cfg, wl.coords, masks)
+    total = int(woffs[-1])
+    ctx = ctx_for(vox, cfg)
+    h0 = np.zeros(total * 96, np.uint8)
+    h1 = np.zeros(total * 24, np.uint8)
+    hoffs = np.zeros(len(coords) + 1, np.uint64)
+    ctx.gen_mesh_host(coords, masks, len(coords), h0, h1, total, hoffs)
+    assert np.array_equal(hoffs, woffs)
+    assert np.array_equal(h0, w0) and np.array_equal(h1, w1)
+    # too small: the status says so and the offsets still give the required size
+    st = ctx.gen_mesh_host(coords, masks, len(coords), h0, h1, total - 1, hoffs,
+                           raise_on_error=False)
+    assert st == vox.VOX_ERR_CAPACITY and int(hoffs[-1]) == total
+    ctx.close()
+
+
+def test_frustum_matches_oracle(vox, oracle):
+    from test_oracle_kat import perspective_look
+    rng = np.random.default_rng(3)
+    cfg = vox.make_config(chunk_size=32)
+    ctx = ctx_for(vox, cfg)
+    coords = rng.integers(-12, 12, (5000, 3)).astype(np.int32)
+    d_coords = to_dev(coords)
+    vis = dev_bytes(len(coords))
+    for t in range(8):
+        eye = rng.uniform(-100, 100, 3)
+        fwd = rng.standard_normal(3)
+        M = perspective_look(eye, fwd, fovy=float(rng.uniform(0.5, 2.0)), far=float(rng.uniform(50, 400)))
+        planes = vox.frustum_planes(M.T.reshape(16))
+        assert np.array_equal(np.array(planes, np.float32), oracle.frustum_planes(M.T.reshape(16)))
+        ctx.frustum_cull(planes, d_coords, len(coords), vis)
+        got = to_np(vis, len(coords))
+        want = np.array([oracle.frustum_contains(planes, tuple(c), 32) for c in coords], np.uint8)
+        assert np.array_equal(got, want)
+        assert 0 < want.sum() < len(coords) or t > 0
+    ctx.close()
+
+
+def test_invalid_arguments_rejected(vox):
+    cfg = vox.make_config(chunk_size=16)
+    ctx = ctx_for(vox, cfg)
+    with pytest.raises(vox.VoxError) as e:
+        ctx.gen_mesh_batch(None, None, 4, None, None, 0, None)
+    assert e.value.status == vox.VOX_ERR_INVALID
+    d_coords = to_dev(np.zeros((2, 3), np.int32))
+    offs = to_dev(np.zeros(3, np.uint64))
+    bad = dev_bytes(4096)
+    with pytest.raises(vox.VoxError):  # misaligned vertex output
+        ctx.gen_mesh_batch(d_coords, None, 2, bad.data_ptr() + 4, bad, 10, offs)
+    ctx.close()

@@ -1,0 +1,595 @@
+// vox_api.cpp — the C ABI (include/voxgpu.h): contexts, argument checks, launches.
+//
+// Host code only; kernels are reached through the KernelSet tables of the per-size
+// translation units. Every CUDA failure becomes a status code plus a message kept in
+// the context; nothing here aborts the process (the reference panics via unwrap where
+// these calls return an error).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "voxgpu.h"
+#include "vox_kernels.h"
+#include "vox_tables.h"
+#include "vox_types.h"
+
+using namespace vox;
+
+struct vox_ctx {
+  vox_config cfg{};
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::mutex mu;
+  const KernelSet* ks = nullptr;
+  GenDev gen{};
+  int gm = GM_HEIGHT;
+  int stage_faces = 0;
+  int batch_grid[4] = {0, 0, 0, 0};  // persistent grid per gen mode
+  TablesDev* d_tables = nullptr;
+  BatchCtl* d_ctl = nullptr;
+  BatchCtl* h_ctl = nullptr;  // pinned
+  unsigned long long* d_state = nullptr;
+  size_t state_cap = 0;
+  unsigned long long launches = 0;
+  // buffers of the host-pointer entry point
+  void* d_in = nullptr;
+  size_t in_cap = 0;
+  unsigned long long* d_offsets = nullptr;
+  size_t offsets_cap = 0;
+  void* d_out0 = nullptr;
+  void* d_out1 = nullptr;
+  size_t out_cap_faces = 0;
+  std::string last_error;
+};
+
+namespace {
+
+int fail(vox_ctx* ctx, int status, const char* fmt, ...) {
+  if (ctx) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    ctx->last_error = buf;
+  }
+  return status;
+}
+
+int cuda_fail(vox_ctx* ctx, cudaError_t e, const char* what) {
+  return fail(ctx, e == cudaErrorMemoryAllocation ? VOX_ERR_OOM : VOX_ERR_CUDA, "%s: %s (%s)",
+              what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+#define VOX_CUDA(ctx, call, what)                  \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return cuda_fail(ctx, e_, what); \
+  } while (0)
+
+const KernelSet* kernel_set_for(int n) {
+  switch (n) {
+    case 8: return &kernel_set_8();
+    case 16: return &kernel_set_16();
+    case 32: return &kernel_set_32();
+    case 64: return &kernel_set_64();
+    default: return nullptr;
+  }
+}
+
+int words_per_chunk(int n) { return n * n * (n > 32 ? n / 32 : 1); }
+int bytes_out0(int layout) { return layout == VOX_LAYOUT_INSTANCED ? 68 : 96; }
+int bytes_out1(int layout) { return layout == VOX_LAYOUT_INSTANCED ? 0 : 24; }
+
+int validate_config(const vox_config* c, std::string* why) {
+  if (!c) {
+    *why = "config is NULL";
+    return VOX_ERR_INVALID;
+  }
+  if (!kernel_set_for(c->chunk_size)) {
+    *why = "chunk_size must be 8, 16, 32 or 64";
+    return VOX_ERR_INVALID;
+  }
+  if (c->cull_mode != VOX_CULL_REFERENCE && c->cull_mode != VOX_CULL_FULL6) {
+    *why = "unknown cull_mode";
+    return VOX_ERR_INVALID;
+  }
+  if (c->layout != VOX_LAYOUT_VERTEX && c->layout != VOX_LAYOUT_INSTANCED) {
+    *why = "unknown layout";
+    return VOX_ERR_INVALID;
+  }
+  const vox_generator& g = c->gen;
+  if (g.kind != VOX_GEN_HEIGHTMAP && g.kind != VOX_GEN_DENSITY && g.kind != VOX_GEN_BERNOULLI) {
+    *why = "unknown generator kind";
+    return VOX_ERR_INVALID;
+  }
+  if (g.kind != VOX_GEN_BERNOULLI && (g.octaves < 1 || g.octaves > 16)) {
+    *why = "octaves must be in 1..16";
+    return VOX_ERR_INVALID;
+  }
+  return VOX_OK;
+}
+
+int gen_mode_of(int kind) {
+  switch (kind) {
+    case VOX_GEN_HEIGHTMAP: return GM_HEIGHT;
+    case VOX_GEN_DENSITY: return GM_DENSITY;
+    default: return GM_BERNOULLI;
+  }
+}
+
+// Largest staging window that keeps two CTAs per SM (at least one full row: 6N faces).
+int default_stage_faces(const KernelSet& ks, int layout) {
+  const int budget = 100 * 1024;
+  const int per = layout == VOX_LAYOUT_INSTANCED ? 68 : 120;
+  int f = (budget - ks.smem_fixed[layout]) / per;
+  f = std::min(f, 4096);
+  f = std::max(f, 6 * ks.n_size);
+  return f;
+}
+
+int prepare_kernel(vox_ctx* ctx, const void* fn, int smem) {
+  VOX_CUDA(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+           "cudaFuncSetAttribute");
+  return VOX_OK;
+}
+
+int ensure_state(vox_ctx* ctx, size_t n) {
+  if (n <= ctx->state_cap) return VOX_OK;
+  size_t cap = std::max<size_t>(n, 1024);
+  if (ctx->d_state) cudaFree(ctx->d_state);
+  ctx->d_state = nullptr;
+  ctx->state_cap = 0;
+  VOX_CUDA(ctx, cudaMalloc(&ctx->d_state, cap * sizeof(unsigned long long)), "cudaMalloc(state)");
+  VOX_CUDA(ctx, cudaMemsetAsync(ctx->d_state, 0, cap * sizeof(unsigned long long), ctx->stream),
+           "cudaMemsetAsync(state)");
+  ctx->state_cap = cap;
+  return VOX_OK;
+}
+
+// Look-back states are tagged with a 24-bit launch epoch; wipe them before a tag can repeat.
+int before_batch_launch(vox_ctx* ctx) {
+  if (ctx->launches > 0 && (ctx->launches & ((1ull << 23) - 1)) == 0 && ctx->d_state) {
+    VOX_CUDA(ctx, cudaMemsetAsync(ctx->d_state, 0, ctx->state_cap * sizeof(unsigned long long),
+                                  ctx->stream),
+             "cudaMemsetAsync(state)");
+  }
+  ++ctx->launches;
+  return VOX_OK;
+}
+
+MeshArgs base_args(vox_ctx* ctx) {
+  MeshArgs a;
+  std::memset(&a, 0, sizeof a);
+  a.tables = ctx->d_tables;
+  a.ctl = ctx->d_ctl;
+  a.state = ctx->d_state;
+  a.gen = ctx->gen;
+  a.full6 = ctx->cfg.cull_mode == VOX_CULL_FULL6 ? 1 : 0;
+  a.stage_faces = ctx->stage_faces;
+  return a;
+}
+
+int launch(vox_ctx* ctx, const void* fn, int grid, int smem, void** params) {
+  VOX_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(ctx->ks->threads), params, (size_t)smem,
+                                 ctx->stream),
+           "cudaLaunchKernel");
+  return VOX_OK;
+}
+
+bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) % a) == 0; }
+
+int check_outputs(vox_ctx* ctx, void* out0, void* out1, uint64_t cap) {
+  if (cap == 0) return VOX_OK;
+  if (!out0) return fail(ctx, VOX_ERR_INVALID, "out0 is NULL with cap_faces > 0");
+  if (ctx->cfg.layout == VOX_LAYOUT_VERTEX) {
+    if (!out1) return fail(ctx, VOX_ERR_INVALID, "out1 (indices) is NULL with cap_faces > 0");
+    if (!aligned(out0, 16) || !aligned(out1, 8))
+      return fail(ctx, VOX_ERR_INVALID, "vertex output must be 16-byte aligned, indices 8-byte");
+  } else if (!aligned(out0, 4)) {
+    return fail(ctx, VOX_ERR_INVALID, "instance output must be 4-byte aligned");
+  }
+  return VOX_OK;
+}
+
+int batch_launch(vox_ctx* ctx, MeshArgs& a, int gm) {
+  int st = ensure_state(ctx, (size_t)a.n);
+  if (st != VOX_OK) return st;
+  st = before_batch_launch(ctx);
+  if (st != VOX_OK) return st;
+  a.state = ctx->d_state;
+  const int layout = ctx->cfg.layout;
+  const void* fn = ctx->ks->batch[gm][layout];
+  const int smem = ctx->ks->smem_total(layout, ctx->stage_faces);
+  const int grid = std::max(1, std::min(a.n, ctx->batch_grid[gm]));
+  void* params[] = {&a};
+  return launch(ctx, fn, grid, smem, params);
+}
+
+}  // namespace
+
+extern "C" {
+
+int vox_abi_version(void) { return VOX_ABI_VERSION; }
+
+const char* vox_status_string(int s) {
+  switch (s) {
+    case VOX_OK: return "ok";
+    case VOX_ERR_INVALID: return "invalid argument";
+    case VOX_ERR_OOM: return "out of memory";
+    case VOX_ERR_CUDA: return "CUDA error";
+    case VOX_ERR_TIMEOUT: return "device wait timed out";
+    case VOX_ERR_CAPACITY: return "output capacity exceeded";
+    case VOX_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+int vox_query_sizes(const vox_config* cfg, vox_sizes* out) {
+  std::string why;
+  if (validate_config(cfg, &why) != VOX_OK || !out) return VOX_ERR_INVALID;
+  const int n = cfg->chunk_size;
+  out->occ_words_per_chunk = (uint32_t)words_per_chunk(n);
+  out->bytes_per_face_out0 = (uint32_t)bytes_out0(cfg->layout);
+  out->bytes_per_face_out1 = (uint32_t)bytes_out1(cfg->layout);
+  out->max_faces_per_chunk = (uint32_t)(3 * n * n * n + 6 * n * n);
+  return VOX_OK;
+}
+
+int vox_ctx_create(const vox_config* cfg, void* stream, vox_ctx** out) {
+  if (!out) return VOX_ERR_INVALID;
+  *out = nullptr;
+  std::string why;
+  if (validate_config(cfg, &why) != VOX_OK) {
+    std::fprintf(stderr, "voxgpu: invalid config: %s\n", why.c_str());
+    return VOX_ERR_INVALID;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return VOX_ERR_NO_DEVICE;
+  }
+  vox_ctx* ctx = new (std::nothrow) vox_ctx();
+  if (!ctx) return VOX_ERR_OOM;
+  ctx->cfg = *cfg;
+  ctx->ks = kernel_set_for(cfg->chunk_size);
+  const vox_generator& g = cfg->gen;
+  ctx->gen.kind = g.kind;
+  ctx->gen.octaves = g.octaves;
+  ctx->gen.seed = g.seed;
+  ctx->gen.freq = g.frequency;
+  ctx->gen.lac = g.lacunarity;
+  ctx->gen.gain = g.gain;
+  ctx->gen.amp = g.amplitude;
+  ctx->gen.base = g.base_height;
+  ctx->gen.y_ref = g.y_ref;
+  ctx->gen.y_scale = g.y_scale;
+  ctx->gen.solid_below_zero = g.solid_below_zero;
+  ctx->gm = gen_mode_of(g.kind);
+  int st = VOX_OK;
+  auto cleanup = [&](int s) {
+    vox_ctx_destroy(ctx);
+    return s;
+  };
+  if (cudaGetDevice(&ctx->device) != cudaSuccess) return cleanup(cuda_fail(ctx, cudaGetLastError(), "cudaGetDevice"));
+  if (cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess)
+    return cleanup(VOX_ERR_CUDA);
+  if (stream) {
+    ctx->stream = static_cast<cudaStream_t>(stream);
+  } else {
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+      return cleanup(VOX_ERR_CUDA);
+    ctx->own_stream = true;
+  }
+  TablesDev tab;
+  build_tables(*cfg, tab);
+  if (cudaMalloc(&ctx->d_tables, sizeof(TablesDev)) != cudaSuccess) return cleanup(VOX_ERR_OOM);
+  if (cudaMemcpy(ctx->d_tables, &tab, sizeof tab, cudaMemcpyHostToDevice) != cudaSuccess)
+    return cleanup(VOX_ERR_CUDA);
+  if (cudaMalloc(&ctx->d_ctl, sizeof(BatchCtl)) != cudaSuccess) return cleanup(VOX_ERR_OOM);
+  if (cudaMemset(ctx->d_ctl, 0, sizeof(BatchCtl)) != cudaSuccess) return cleanup(VOX_ERR_CUDA);
+  if (cudaMallocHost(&ctx->h_ctl, sizeof(BatchCtl)) != cudaSuccess) return cleanup(VOX_ERR_OOM);
+  ctx->stage_faces = default_stage_faces(*ctx->ks, cfg->layout);
+  // Kernel attributes and the persistent grid (resident CTAs per SM x SMs).
+  const int layout = cfg->layout;
+  const int smem = ctx->ks->smem_total(layout, ctx->stage_faces);
+  for (int gm = 0; gm < 4; ++gm) {
+    const void* fn = ctx->ks->batch[gm][layout];
+    if ((st = prepare_kernel(ctx, fn, smem)) != VOX_OK) return cleanup(st);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, ctx->ks->threads, smem) != cudaSuccess || per_sm < 1)
+      return cleanup(fail(ctx, VOX_ERR_CUDA, "kernel does not fit on an SM"));
+    ctx->batch_grid[gm] = per_sm * ctx->num_sms;
+  }
+  if ((st = prepare_kernel(ctx, ctx->ks->single[layout], smem)) != VOX_OK) return cleanup(st);
+  const int gsmem = ctx->ks->smem_total(VOX_LAYOUT_VERTEX, 1);
+  for (int gm = 1; gm < 4; ++gm)
+    if ((st = prepare_kernel(ctx, ctx->ks->generate[gm], gsmem)) != VOX_OK) return cleanup(st);
+  if ((st = ensure_state(ctx, 1024)) != VOX_OK) return cleanup(st);
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return cleanup(VOX_ERR_CUDA);
+  *out = ctx;
+  return VOX_OK;
+}
+
+int vox_ctx_destroy(vox_ctx* ctx) {
+  if (!ctx) return VOX_OK;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  cudaFree(ctx->d_tables);
+  cudaFree(ctx->d_ctl);
+  cudaFree(ctx->d_state);
+  cudaFree(ctx->d_in);
+  cudaFree(ctx->d_offsets);
+  cudaFree(ctx->d_out0);
+  cudaFree(ctx->d_out1);
+  if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return VOX_OK;
+}
+
+void* vox_ctx_stream(vox_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+const char* vox_ctx_last_error(vox_ctx* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+static int sync_locked(vox_ctx* ctx) {
+  VOX_CUDA(ctx, cudaMemcpyAsync(ctx->h_ctl, ctx->d_ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost,
+                                ctx->stream),
+           "cudaMemcpyAsync(ctl)");
+  VOX_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  const unsigned err = ctx->h_ctl->err;
+  if (err == 0) return VOX_OK;
+  VOX_CUDA(ctx, cudaMemsetAsync(&ctx->d_ctl->err, 0, sizeof(unsigned), ctx->stream),
+           "cudaMemsetAsync(err)");
+  VOX_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  if (err & ERR_TIMEOUT) return fail(ctx, VOX_ERR_TIMEOUT, "a device-side look-back wait gave up");
+  if (err & ERR_BAD_INPUT) return fail(ctx, VOX_ERR_INVALID, "a slot index was out of range");
+  return fail(ctx, VOX_ERR_CAPACITY, "output capacity exceeded");
+}
+
+int vox_ctx_sync(vox_ctx* ctx) {
+  if (!ctx) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  return sync_locked(ctx);
+}
+
+int vox_generate(vox_ctx* ctx, const vox_chunk_coord* d_coords, int32_t n,
+                 int64_t chunk_index_base, uint32_t* d_occ) {
+  if (!ctx) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (n < 0 || (n > 0 && (!d_coords || !d_occ))) return fail(ctx, VOX_ERR_INVALID, "bad arguments");
+  if (n == 0) return VOX_OK;
+  MeshArgs a = base_args(ctx);
+  a.n = n;
+  a.index_base = chunk_index_base;
+  a.coords = d_coords;
+  uint32_t* occ = d_occ;
+  void* params[] = {&a, &occ};
+  return launch(ctx, ctx->ks->generate[ctx->gm], n, ctx->ks->smem_total(VOX_LAYOUT_VERTEX, 1),
+                params);
+}
+
+int vox_occ_to_cubes(vox_ctx* ctx, const uint32_t* d_occ, int32_t n, uint8_t* d_cubes) {
+  if (!ctx) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (n < 0 || (n > 0 && (!d_occ || !d_cubes))) return fail(ctx, VOX_ERR_INVALID, "bad arguments");
+  VOX_CUDA(ctx, launch_occ_to_cubes(d_occ, n, ctx->cfg.chunk_size, d_cubes, ctx->stream),
+           "occ_to_cubes");
+  return VOX_OK;
+}
+
+int vox_cubes_to_occ(vox_ctx* ctx, const uint8_t* d_cubes, int32_t n, uint32_t* d_occ) {
+  if (!ctx) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (n < 0 || (n > 0 && (!d_occ || !d_cubes))) return fail(ctx, VOX_ERR_INVALID, "bad arguments");
+  VOX_CUDA(ctx, launch_cubes_to_occ(d_cubes, n, ctx->cfg.chunk_size, d_occ, ctx->stream),
+           "cubes_to_occ");
+  return VOX_OK;
+}
+
+int vox_mesh(vox_ctx* ctx, const uint32_t* d_occ, const uint32_t* const d_nbr[6],
+             vox_chunk_coord coord, void* d_out0, void* d_out1, uint64_t cap_faces,
+             uint64_t* d_face_count) {
+  if (!ctx) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!d_occ || !d_face_count) return fail(ctx, VOX_ERR_INVALID, "d_occ and d_face_count are required");
+  int st = check_outputs(ctx, d_out0, d_out1, cap_faces);
+  if (st != VOX_OK) return st;
+  MeshArgs a = base_args(ctx);
+  a.n = 1;
+  a.occ_self = d_occ;
+  for (int d = 0; d < 6; ++d) a.occ_nbr[d] = d_nbr ? d_nbr[d] : nullptr;
+  a.coord_single = coord;
+  a.out0 = d_out0;
+  a.out1 = d_out1;
+  a.cap = cap_faces;
+  a.face_offsets = reinterpret_cast<unsigned long long*>(d_face_count);
+  void* params[] = {&a};
+  const int layout = ctx->cfg.layout;
+  return launch(ctx, ctx->ks->single[layout], 1, ctx->ks->smem_total(layout, ctx->stage_faces),
+                params);
+}
+
+int vox_mesh_batch(vox_ctx* ctx, const uint32_t* d_occ_pool, int32_t pool_slots,
+                   const int32_t* d_slots, const int32_t* d_nbr_slots,
+                   const vox_chunk_coord* d_coords, int32_t n, void* d_out0, void* d_out1,
+                   uint64_t cap_faces, uint64_t* d_face_offsets) {
+  if (!ctx) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (n < 0 || (n > 0 && (!d_occ_pool || !d_slots || !d_coords || !d_face_offsets)) ||
+      pool_slots < 1)
+    return fail(ctx, VOX_ERR_INVALID, "bad arguments");
+  if (n == 0) return VOX_OK;
+  int st = check_outputs(ctx, d_out0, d_out1, cap_faces);
+  if (st != VOX_OK) return st;
+  MeshArgs a = base_args(ctx);
+  a.n = n;
+  a.coords = d_coords;
+  a.occ_pool = d_occ_pool;
+  a.pool_slots = pool_slots;
+  a.slots = d_slots;
+  a.nbr_slots = d_nbr_slots;
+  a.out0 = d_out0;
+  a.out1 = d_out1;
+  a.cap = cap_faces;
+  a.face_offsets = reinterpret_cast<unsigned long long*>(d_face_offsets);
+  return batch_launch(ctx, a, GM_OCC);
+}
+
+int vox_gen_mesh_batch(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
+                       int32_t n, int64_t chunk_index_base, void* d_out0, void* d_out1,
+                       uint64_t cap_faces, uint64_t* d_face_offsets) {
+  if (!ctx) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (n < 0 || (n > 0 && (!d_coords || !d_face_offsets)))
+    return fail(ctx, VOX_ERR_INVALID, "bad arguments");
+  if (n == 0) return VOX_OK;
+  int st = check_outputs(ctx, d_out0, d_out1, cap_faces);
+  if (st != VOX_OK) return st;
+  MeshArgs a = base_args(ctx);
+  a.n = n;
+  a.index_base = chunk_index_base;
+  a.coords = d_coords;
+  a.nbr_mask = d_nbr_mask;
+  a.out0 = d_out0;
+  a.out1 = d_out1;
+  a.cap = cap_faces;
+  a.face_offsets = reinterpret_cast<unsigned long long*>(d_face_offsets);
+  return batch_launch(ctx, a, ctx->gm);
+}
+
+static int grow(vox_ctx* ctx, void** p, size_t* cap, size_t need, const char* what) {
+  if (need <= *cap) return VOX_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  VOX_CUDA(ctx, cudaMalloc(p, need), what);
+  *cap = need;
+  return VOX_OK;
+}
+
+int vox_gen_mesh_host(vox_ctx* ctx, const vox_chunk_coord* h_coords, const uint8_t* h_nbr_mask,
+                      int32_t n, int64_t chunk_index_base, void* h_out0, void* h_out1,
+                      uint64_t cap_faces, uint64_t* h_face_offsets) {
+  if (!ctx) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (n < 0 || (n > 0 && (!h_coords || !h_face_offsets)))
+    return fail(ctx, VOX_ERR_INVALID, "bad arguments");
+  if (cap_faces > 0 && (!h_out0 || (ctx->cfg.layout == VOX_LAYOUT_VERTEX && !h_out1)))
+    return fail(ctx, VOX_ERR_INVALID, "output buffers are NULL with cap_faces > 0");
+  if (n == 0) return VOX_OK;
+  const int layout = ctx->cfg.layout;
+  const size_t b0 = (size_t)bytes_out0(layout), b1 = (size_t)bytes_out1(layout);
+  const size_t in_bytes = (size_t)n * sizeof(vox_chunk_coord) + (h_nbr_mask ? (size_t)n : 0);
+  int st;
+  if ((st = grow(ctx, &ctx->d_in, &ctx->in_cap, in_bytes, "cudaMalloc(inputs)")) != VOX_OK) return st;
+  size_t off_cap = ctx->offsets_cap * sizeof(unsigned long long);
+  void* offp = ctx->d_offsets;
+  if ((st = grow(ctx, &offp, &off_cap, ((size_t)n + 1) * sizeof(unsigned long long),
+                 "cudaMalloc(offsets)")) != VOX_OK)
+    return st;
+  ctx->d_offsets = static_cast<unsigned long long*>(offp);
+  ctx->offsets_cap = off_cap / sizeof(unsigned long long);
+  if (cap_faces > ctx->out_cap_faces) {
+    cudaFree(ctx->d_out0);
+    cudaFree(ctx->d_out1);
+    ctx->d_out0 = ctx->d_out1 = nullptr;
+    ctx->out_cap_faces = 0;
+    VOX_CUDA(ctx, cudaMalloc(&ctx->d_out0, cap_faces * b0), "cudaMalloc(out0)");
+    if (b1) VOX_CUDA(ctx, cudaMalloc(&ctx->d_out1, cap_faces * b1), "cudaMalloc(out1)");
+    ctx->out_cap_faces = cap_faces;
+  }
+  vox_chunk_coord* d_coords = static_cast<vox_chunk_coord*>(ctx->d_in);
+  uint8_t* d_mask = h_nbr_mask ? reinterpret_cast<uint8_t*>(d_coords + n) : nullptr;
+  VOX_CUDA(ctx, cudaMemcpyAsync(d_coords, h_coords, (size_t)n * sizeof(vox_chunk_coord),
+                                cudaMemcpyHostToDevice, ctx->stream),
+           "H2D coords");
+  if (h_nbr_mask)
+    VOX_CUDA(ctx, cudaMemcpyAsync(d_mask, h_nbr_mask, (size_t)n, cudaMemcpyHostToDevice, ctx->stream),
+             "H2D mask");
+  MeshArgs a = base_args(ctx);
+  a.n = n;
+  a.index_base = chunk_index_base;
+  a.coords = d_coords;
+  a.nbr_mask = d_mask;
+  a.out0 = ctx->d_out0;
+  a.out1 = ctx->d_out1;
+  a.cap = cap_faces;
+  a.face_offsets = ctx->d_offsets;
+  if ((st = batch_launch(ctx, a, ctx->gm)) != VOX_OK) return st;
+  VOX_CUDA(ctx, cudaMemcpyAsync(h_face_offsets, ctx->d_offsets, ((size_t)n + 1) * sizeof(uint64_t),
+                                cudaMemcpyDeviceToHost, ctx->stream),
+           "D2H offsets");
+  VOX_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  const uint64_t total = h_face_offsets[n];
+  const uint64_t w = std::min<uint64_t>(total, cap_faces);
+  if (w > 0) {
+    VOX_CUDA(ctx, cudaMemcpyAsync(h_out0, ctx->d_out0, w * b0, cudaMemcpyDeviceToHost, ctx->stream),
+             "D2H out0");
+    if (b1)
+      VOX_CUDA(ctx, cudaMemcpyAsync(h_out1, ctx->d_out1, w * b1, cudaMemcpyDeviceToHost, ctx->stream),
+               "D2H out1");
+  }
+  st = sync_locked(ctx);
+  if (st == VOX_OK && total > cap_faces)
+    st = fail(ctx, VOX_ERR_CAPACITY, "output capacity exceeded: %llu faces needed",
+              (unsigned long long)total);
+  return st;
+}
+
+int vox_frustum_planes(const float m[16], float planes[24]) {
+  if (!m || !planes) return VOX_ERR_INVALID;
+  // data[col][row] of the column-major matrix (src/frustum_culling.rs:54-83).
+  auto D = [&](int c, int r) { return m[c * 4 + r]; };
+  float p[6][4];
+  for (int c = 0; c < 4; ++c) {
+    p[2][c] = D(c, 3) + D(c, 0);  // left
+    p[3][c] = D(c, 3) - D(c, 0);  // right
+    p[4][c] = D(c, 3) - D(c, 1);  // top
+    p[5][c] = D(c, 3) + D(c, 1);  // bottom
+    p[0][c] = D(c, 3) + D(c, 2);  // near
+    p[1][c] = D(c, 3) - D(c, 2);  // far
+  }
+  for (int k = 0; k < 6; ++k)
+    for (int c = 0; c < 4; ++c) planes[4 * k + c] = p[k][c];
+  return VOX_OK;
+}
+
+int vox_frustum_cull(vox_ctx* ctx, const float planes[24], const vox_chunk_coord* d_coords,
+                     int32_t n, uint8_t* d_visible) {
+  if (!ctx) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!planes || n < 0 || (n > 0 && (!d_coords || !d_visible)))
+    return fail(ctx, VOX_ERR_INVALID, "bad arguments");
+  Planes pl;
+  std::memcpy(pl.p, planes, sizeof pl.p);
+  VOX_CUDA(ctx, launch_frustum(pl, d_coords, n, ctx->cfg.chunk_size, d_visible, ctx->stream),
+           "frustum");
+  return VOX_OK;
+}
+
+int vox_host_alloc(size_t bytes, void** out) {
+  if (!out) return VOX_ERR_INVALID;
+  *out = nullptr;
+  if (bytes == 0) return VOX_OK;
+  cudaError_t e = cudaMallocHost(out, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    return VOX_ERR_OOM;
+  }
+  return VOX_OK;
+}
+
+int vox_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+  return VOX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,10 @@
+// Kernel instantiations for chunk size N = 16 (one translation unit per size so the
+// build compiles them in parallel).
+#include "vox_kernel_set.cuh"
+
+namespace vox {
+const KernelSet& kernel_set_16() {
+  static const KernelSet k = make_kernel_set<16>();
+  return k;
+}
+}  // namespace vox

@@ -1,0 +1,110 @@
+// vox_misc.cu — small kernels around the hot path: the chunk-frustum test and the
+// conversions between occupancy bitmasks and the reference's one-byte-per-voxel cubes.
+#include <cstdint>
+
+#include "voxgpu.h"
+#include "vox_kernels.h"
+
+namespace vox {
+
+namespace {
+
+constexpr uint8_t kGrass = 0;  // CubeType::GRASS (src/cube.rs:17-21)
+constexpr uint8_t kAir = 2;    // CubeType::AIR
+
+// One thread per voxel: cubes[x + N*z + N*N*y] from bit x of row (y, z).
+__global__ void k_occ_to_cubes(const uint32_t* __restrict__ occ, long long total, int n_size,
+                               uint8_t* __restrict__ cubes) {
+  const int W = n_size > 32 ? n_size / 32 : 1;
+  const long long per = (long long)n_size * n_size * n_size;
+  for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < total;
+       v += (long long)gridDim.x * blockDim.x) {
+    const long long c = v / per;
+    const int i = (int)(v - c * per);
+    const int x = i % n_size, z = (i / n_size) % n_size, y = i / (n_size * n_size);
+    const uint32_t w = occ[c * (long long)n_size * n_size * W + (long long)(y * n_size + z) * W + (x >> 5)];
+    cubes[v] = ((w >> (x & 31)) & 1u) ? kGrass : kAir;
+  }
+}
+
+// One thread per occupancy word: a voxel is solid iff its byte is not AIR (chunk.rs:71).
+__global__ void k_cubes_to_occ(const uint8_t* __restrict__ cubes, long long words, int n_size,
+                               uint32_t* __restrict__ occ) {
+  const int W = n_size > 32 ? n_size / 32 : 1;
+  const int bits = n_size < 32 ? n_size : 32;
+  const long long per_words = (long long)n_size * n_size * W;
+  const long long per = (long long)n_size * n_size * n_size;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < words;
+       q += (long long)gridDim.x * blockDim.x) {
+    const long long c = q / per_words;
+    const int k = (int)(q - c * per_words);
+    const int row = k / W, w = k % W;
+    const int y = row / n_size, z = row % n_size;
+    const uint8_t* src = cubes + c * per + (long long)n_size * z + (long long)n_size * n_size * y + w * 32;
+    uint32_t v = 0;
+    for (int b = 0; b < bits; ++b) v |= (src[b] != kAir ? 1u : 0u) << b;
+    occ[q] = v;
+  }
+}
+
+// Frustum::contains (src/frustum_culling.rs:16-40) per chunk: corners in the reference's
+// order, planes near, far, left, right, top, bottom; dist = ((a*x + b*y) + c*z) + d with
+// one rounding per operation (the file is built with -fmad=false).
+__global__ void k_frustum(Planes pl, const vox_chunk_coord* __restrict__ coords, int n, int extent,
+                          uint8_t* __restrict__ visible) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const vox_chunk_coord c = coords[i];
+  const float px = (float)(c.x * extent), py = (float)(c.y * extent), pz = (float)(c.z * extent);
+  const float e = (float)extent;
+  uint8_t inside_any = 0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const float x = (k & 1) ? px + e : px;
+    const float z = (k & 2) ? pz + e : pz;
+    const float y = (k & 4) ? py + e : py;
+    bool inside = true;
+#pragma unroll
+    for (int j = 0; j < 6; ++j) {
+      const float d = pl.p[4 * j] * x + pl.p[4 * j + 1] * y + pl.p[4 * j + 2] * z + pl.p[4 * j + 3];
+      inside = inside && !(d < 0.0f);
+    }
+    inside_any |= inside ? 1 : 0;
+  }
+  visible[i] = inside_any;
+}
+
+int grid_for(long long work, int threads) {
+  long long g = (work + threads - 1) / threads;
+  if (g > 152LL * 32) g = 152LL * 32;
+  return g < 1 ? 1 : (int)g;
+}
+
+}  // namespace
+
+cudaError_t launch_occ_to_cubes(const uint32_t* occ, int n, int n_size, uint8_t* cubes,
+                                cudaStream_t st) {
+  const long long total = (long long)n * n_size * n_size * n_size;
+  if (total == 0) return cudaSuccess;
+  k_occ_to_cubes<<<grid_for(total, 256), 256, 0, st>>>(occ, total, n_size, cubes);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cubes_to_occ(const uint8_t* cubes, int n, int n_size, uint32_t* occ,
+                                cudaStream_t st) {
+  const int W = n_size > 32 ? n_size / 32 : 1;
+  const long long words = (long long)n * n_size * n_size * W;
+  if (words == 0) return cudaSuccess;
+  k_cubes_to_occ<<<grid_for(words, 256), 256, 0, st>>>(cubes, words, n_size, occ);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_frustum(const Planes& planes, const void* coords, int n, int extent,
+                           uint8_t* visible, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  k_frustum<<<(n + 255) / 256, 256, 0, st>>>(planes, static_cast<const vox_chunk_coord*>(coords),
+                                              n, extent, visible);
+  return cudaGetLastError();
+}
+
+}  // namespace vox

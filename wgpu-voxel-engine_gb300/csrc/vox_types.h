@@ -1,0 +1,70 @@
+// vox_types.h — structures shared by the host code and the kernels (plain C++).
+#pragma once
+
+#include <cstdint>
+#include <type_traits>
+
+#include "voxgpu.h"
+
+namespace vox {
+
+constexpr unsigned ERR_TIMEOUT = 1u;   // a look-back wait gave up
+constexpr unsigned ERR_CAPACITY = 2u;  // output capacity exceeded
+constexpr unsigned ERR_BAD_INPUT = 4u; // a slot index out of range
+
+// Bounded spin: ~2^22 polls with a growing nanosleep (well under 2 s in total).
+constexpr int kSpinLimit = 1 << 22;
+
+enum GenMode : int { GM_OCC = 0, GM_HEIGHT = 1, GM_DENSITY = 2, GM_BERNOULLI = 3 };
+
+struct GenDev {
+  int kind;
+  int octaves;
+  unsigned long long seed;
+  float freq, lac, gain, amp, base, y_ref, y_scale;
+  int solid_below_zero;
+};
+
+// Per-context constant tables, computed on the host once (see vox_tables.cpp).
+struct TablesDev {
+  float corner[6][4][3];  // rotated quad corner offsets per emission direction
+  float part[6][3][3];    // T*R entries (i<3, j<3) before the t_i * 0 term
+  float row3[6][3];       // T*R row 3, columns 0..2
+  float uv[4][2];         // quad::VERTICES tex coords
+  uint32_t tex[6];        // texture index per emission direction
+  uint32_t slot[6];       // face slot per emission direction
+  uint8_t perm[512];      // noise permutation
+};
+
+struct BatchCtl {
+  unsigned int next;   // work-queue ticket; reset to 0 by the last CTA of a launch
+  unsigned int epoch;  // look-back state tag; advanced by the last CTA of a launch
+  unsigned int err;    // ERR_* bits, sticky until the host clears them
+  unsigned int pad;
+};
+
+struct MeshArgs {
+  int n;
+  long long index_base;
+  const vox_chunk_coord* coords;
+  const uint8_t* nbr_mask;
+  const uint32_t* occ_pool;   // GM_OCC, batch: chunk i at occ_pool + slots[i] * words
+  const int32_t* slots;
+  const int32_t* nbr_slots;   // 6 per chunk, -1 = not loaded
+  int pool_slots;             // number of slots in occ_pool (bounds check)
+  const uint32_t* occ_self;   // GM_OCC, single chunk
+  const uint32_t* occ_nbr[6];
+  vox_chunk_coord coord_single;
+  void* out0;
+  void* out1;
+  unsigned long long cap;
+  unsigned long long* face_offsets;  // n + 1 entries (single chunk: the count at [0])
+  unsigned long long* state;         // look-back states, n entries
+  BatchCtl* ctl;
+  const TablesDev* tables;
+  GenDev gen;
+  int full6;
+  int stage_faces;                   // faces per staging window
+};
+
+}  // namespace vox

@@ -1,0 +1,338 @@
+"""voxgpu — Python bindings of the C ABI in include/voxgpu.h (ctypes).
+
+The product is the CUDA library ``libvoxgpu.so`` built in this directory; these
+bindings only marshal arguments. There is no CPU fallback: if the library is missing
+or no GPU is visible, calls raise.
+
+Device buffers are passed as integers (raw device pointers) or as objects with a
+``data_ptr()`` method (torch tensors), so PyTorch can provide device memory and
+streams without appearing in any signature.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+
+from . import _build
+
+__all__ = [
+    "VOX_OK", "VOX_ERR_INVALID", "VOX_ERR_OOM", "VOX_ERR_CUDA", "VOX_ERR_TIMEOUT",
+    "VOX_ERR_CAPACITY", "VOX_ERR_NO_DEVICE", "GEN_HEIGHTMAP", "GEN_DENSITY", "GEN_BERNOULLI",
+    "CULL_REFERENCE", "CULL_FULL6", "LAYOUT_VERTEX", "LAYOUT_INSTANCED", "ChunkCoord",
+    "Generator", "Config", "Sizes", "VoxError", "lib", "Context", "GRASS_TEXTURES",
+    "frustum_planes", "neighbour_masks", "grid_coords",
+]
+
+VOX_OK, VOX_ERR_INVALID, VOX_ERR_OOM, VOX_ERR_CUDA = 0, 1, 2, 3
+VOX_ERR_TIMEOUT, VOX_ERR_CAPACITY, VOX_ERR_NO_DEVICE = 4, 5, 6
+GEN_HEIGHTMAP, GEN_DENSITY, GEN_BERNOULLI = 0, 1, 2
+CULL_REFERENCE, CULL_FULL6 = 0, 1
+LAYOUT_VERTEX, LAYOUT_INSTANCED = 0, 1
+# TEXTURE_INDEX_LIST row of GRASS (src/texture.rs:240-243), by face slot L R Bk F Up Down.
+GRASS_TEXTURES = (0, 0, 0, 0, 2, 1)
+
+
+class ChunkCoord(ctypes.Structure):
+    """ChunkCoord3D (src/coordinate.rs:146-151)."""
+    _fields_ = [("x", ctypes.c_int32), ("y", ctypes.c_int32), ("z", ctypes.c_int32)]
+
+
+class Generator(ctypes.Structure):
+    _fields_ = [
+        ("kind", ctypes.c_int32), ("octaves", ctypes.c_int32), ("seed", ctypes.c_uint64),
+        ("frequency", ctypes.c_float), ("lacunarity", ctypes.c_float), ("gain", ctypes.c_float),
+        ("amplitude", ctypes.c_float), ("base_height", ctypes.c_float), ("y_ref", ctypes.c_float),
+        ("y_scale", ctypes.c_float), ("solid_below_zero", ctypes.c_int32),
+    ]
+
+
+class Config(ctypes.Structure):
+    _fields_ = [
+        ("chunk_size", ctypes.c_int32), ("cull_mode", ctypes.c_int32), ("layout", ctypes.c_int32),
+        ("texture_index", ctypes.c_uint32 * 6), ("gen", Generator),
+    ]
+
+
+class Sizes(ctypes.Structure):
+    _fields_ = [
+        ("occ_words_per_chunk", ctypes.c_uint32), ("bytes_per_face_out0", ctypes.c_uint32),
+        ("bytes_per_face_out1", ctypes.c_uint32), ("max_faces_per_chunk", ctypes.c_uint32),
+    ]
+
+
+class VoxError(RuntimeError):
+    def __init__(self, status: int, what: str, detail: str = ""):
+        self.status = status
+        msg = f"{what}: status {status}"
+        if detail:
+            msg += f" ({detail})"
+        super().__init__(msg)
+
+
+_LIB = None
+
+# Exported functions: name -> (restype, argtypes).
+_P = ctypes.c_void_p
+_SIGS = {
+    "vox_abi_version": (ctypes.c_int, []),
+    "vox_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "vox_query_sizes": (ctypes.c_int, [ctypes.POINTER(Config), ctypes.POINTER(Sizes)]),
+    "vox_ctx_create": (ctypes.c_int, [ctypes.POINTER(Config), _P, ctypes.POINTER(_P)]),
+    "vox_ctx_destroy": (ctypes.c_int, [_P]),
+    "vox_ctx_sync": (ctypes.c_int, [_P]),
+    "vox_ctx_stream": (_P, [_P]),
+    "vox_ctx_last_error": (ctypes.c_char_p, [_P]),
+    "vox_generate": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int64, _P]),
+    "vox_occ_to_cubes": (ctypes.c_int, [_P, _P, ctypes.c_int32, _P]),
+    "vox_cubes_to_occ": (ctypes.c_int, [_P, _P, ctypes.c_int32, _P]),
+    "vox_mesh": (ctypes.c_int, [_P, _P, ctypes.POINTER(_P), ChunkCoord, _P, _P, ctypes.c_uint64,
+                                _P]),
+    "vox_mesh_batch": (ctypes.c_int, [_P, _P, ctypes.c_int32, _P, _P, _P, ctypes.c_int32, _P, _P,
+                                      ctypes.c_uint64, _P]),
+    "vox_gen_mesh_batch": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, ctypes.c_int64, _P, _P,
+                                          ctypes.c_uint64, _P]),
+    "vox_gen_mesh_host": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, ctypes.c_int64, _P, _P,
+                                         ctypes.c_uint64, _P]),
+    "vox_frustum_planes": (ctypes.c_int, [_P, _P]),
+    "vox_frustum_cull": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P]),
+    "vox_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_P)]),
+    "vox_host_free": (ctypes.c_int, [_P]),
+}
+
+
+def lib(build_if_missing: bool = False) -> ctypes.CDLL:
+    """Loads libvoxgpu.so from this directory (raises if it was not built)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB_PATH
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"{path} is missing: run __graft_entry__.build() first")
+        _build.build_library()
+    handle = ctypes.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(handle, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = handle
+    return handle
+
+
+def _ptr(x) -> int:
+    if x is None:
+        return 0
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return int(x.data_ptr())
+    if isinstance(x, ctypes.Array) or isinstance(x, ctypes.Structure):
+        return ctypes.addressof(x)
+    if hasattr(x, "ctypes"):  # numpy array
+        return int(x.ctypes.data)
+    raise TypeError(f"cannot take a pointer of {type(x)!r}")
+
+
+def make_config(chunk_size=32, cull_mode=CULL_REFERENCE, layout=LAYOUT_VERTEX, kind=GEN_HEIGHTMAP,
+                octaves=1, seed=42, frequency=1.0 / 64, lacunarity=2.0, gain=0.5, amplitude=12.0,
+                base_height=4.0, y_ref=0.0, y_scale=0.0, solid_below_zero=0,
+                textures=GRASS_TEXTURES) -> Config:
+    cfg = Config()
+    cfg.chunk_size = chunk_size
+    cfg.cull_mode = cull_mode
+    cfg.layout = layout
+    for i, t in enumerate(textures):
+        cfg.texture_index[i] = t
+    g = cfg.gen
+    g.kind, g.octaves, g.seed = kind, octaves, seed
+    g.frequency, g.lacunarity, g.gain = frequency, lacunarity, gain
+    g.amplitude, g.base_height, g.y_ref, g.y_scale = amplitude, base_height, y_ref, y_scale
+    g.solid_below_zero = solid_below_zero
+    return cfg
+
+
+def query_sizes(cfg: Config) -> Sizes:
+    s = Sizes()
+    st = lib().vox_query_sizes(ctypes.byref(cfg), ctypes.byref(s))
+    if st != VOX_OK:
+        raise VoxError(st, "vox_query_sizes")
+    return s
+
+
+def frustum_planes(m_colmajor) -> list:
+    """Frustum::matrix_to_planes (src/frustum_culling.rs:47-85) via the C ABI."""
+    m = (ctypes.c_float * 16)(*[float(v) for v in m_colmajor])
+    out = (ctypes.c_float * 24)()
+    st = lib().vox_frustum_planes(ctypes.addressof(m), ctypes.addressof(out))
+    if st != VOX_OK:
+        raise VoxError(st, "vox_frustum_planes")
+    return list(out)
+
+
+class Context:
+    """One vox_ctx (one config, one stream)."""
+
+    def __init__(self, cfg: Config, stream: int | None = None):
+        self.cfg = cfg
+        self._lib = lib()
+        h = _P()
+        st = self._lib.vox_ctx_create(ctypes.byref(cfg), _P(stream or 0), ctypes.byref(h))
+        if st != VOX_OK:
+            raise VoxError(st, "vox_ctx_create")
+        self._h = h
+        self.sizes = query_sizes(cfg)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.vox_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def stream(self) -> int:
+        return int(self._lib.vox_ctx_stream(self._h) or 0)
+
+    def _check(self, st: int, what: str):
+        if st != VOX_OK:
+            detail = (self._lib.vox_ctx_last_error(self._h) or b"").decode()
+            raise VoxError(st, what, detail)
+
+    def sync(self, raise_on_error: bool = True) -> int:
+        st = self._lib.vox_ctx_sync(self._h)
+        if raise_on_error:
+            self._check(st, "vox_ctx_sync")
+        return st
+
+    # Chunk::new
+    def generate(self, d_coords, n: int, d_occ, chunk_index_base: int = 0):
+        self._check(self._lib.vox_generate(self._h, _ptr(d_coords), n, chunk_index_base,
+                                           _ptr(d_occ)), "vox_generate")
+
+    def occ_to_cubes(self, d_occ, n: int, d_cubes):
+        self._check(self._lib.vox_occ_to_cubes(self._h, _ptr(d_occ), n, _ptr(d_cubes)),
+                    "vox_occ_to_cubes")
+
+    def cubes_to_occ(self, d_cubes, n: int, d_occ):
+        self._check(self._lib.vox_cubes_to_occ(self._h, _ptr(d_cubes), n, _ptr(d_occ)),
+                    "vox_cubes_to_occ")
+
+    # Chunk::create_mesh
+    def mesh(self, d_occ, nbrs, coord, d_out0, d_out1, cap_faces: int, d_count):
+        arr = (_P * 6)(*[_P(_ptr(b)) for b in (list(nbrs) + [None] * 6)[:6]])
+        c = ChunkCoord(*coord)
+        self._check(self._lib.vox_mesh(self._h, _ptr(d_occ), arr, c, _ptr(d_out0), _ptr(d_out1),
+                                       cap_faces, _ptr(d_count)), "vox_mesh")
+
+    def mesh_batch(self, d_pool, pool_slots: int, d_slots, d_nbr_slots, d_coords, n: int, d_out0,
+                   d_out1, cap_faces: int, d_offsets):
+        self._check(self._lib.vox_mesh_batch(self._h, _ptr(d_pool), pool_slots, _ptr(d_slots),
+                                             _ptr(d_nbr_slots), _ptr(d_coords), n, _ptr(d_out0),
+                                             _ptr(d_out1), cap_faces, _ptr(d_offsets)),
+                    "vox_mesh_batch")
+
+    def gen_mesh_batch(self, d_coords, d_nbr_mask, n: int, d_out0, d_out1, cap_faces: int,
+                       d_offsets, chunk_index_base: int = 0):
+        self._check(self._lib.vox_gen_mesh_batch(self._h, _ptr(d_coords), _ptr(d_nbr_mask), n,
+                                                 chunk_index_base, _ptr(d_out0), _ptr(d_out1),
+                                                 cap_faces, _ptr(d_offsets)),
+                    "vox_gen_mesh_batch")
+
+    def gen_mesh_host(self, h_coords, h_nbr_mask, n: int, h_out0, h_out1, cap_faces: int,
+                      h_offsets, chunk_index_base: int = 0, raise_on_error: bool = True) -> int:
+        st = self._lib.vox_gen_mesh_host(self._h, _ptr(h_coords), _ptr(h_nbr_mask), n,
+                                         chunk_index_base, _ptr(h_out0), _ptr(h_out1), cap_faces,
+                                         _ptr(h_offsets))
+        if raise_on_error:
+            self._check(st, "vox_gen_mesh_host")
+        return st
+
+    def frustum_cull(self, planes, d_coords, n: int, d_visible):
+        p = (ctypes.c_float * 24)(*[float(v) for v in planes])
+        self._check(self._lib.vox_frustum_cull(self._h, ctypes.addressof(p), _ptr(d_coords), n,
+                                               _ptr(d_visible)), "vox_frustum_cull")
+
+
+def grid_coords(xs, ys, zs):
+    """Chunk coordinates of a box, in y-major then z then x order (row-major over y, z, x)."""
+    return [(x, y, z) for y in ys for z in zs for x in xs]
+
+
+def neighbour_masks(coords, full6: bool = False):
+    """Bit d set iff the neighbour in direction d (-x, +x, -z, +z, -y, +y) is in `coords`
+    (the World.chunks lookup of src/chunk_builder.rs:134-169)."""
+    present = set(map(tuple, coords))
+    offs = [(-1, 0, 0), (1, 0, 0), (0, 0, -1), (0, 0, 1), (0, -1, 0), (0, 1, 0)]
+    out = []
+    for (x, y, z) in coords:
+        m = 0
+        for d, (dx, dy, dz) in enumerate(offs):
+            if d >= 4 and not full6:
+                continue
+            if (x + dx, y + dy, z + dz) in present:
+                m |= 1 << d
+        out.append(m)
+    return out
+
+
+@dataclass(frozen=True)
+class Workload:
+    """A named synthetic workload (chunk coordinates + generator config)."""
+    name: str
+    cfg_kwargs: dict
+    coords: tuple
+    index_base: int = 0
+    isolated: bool = False
+
+    def config(self, layout=LAYOUT_VERTEX, cull_mode=CULL_REFERENCE) -> Config:
+        kw = dict(self.cfg_kwargs)
+        kw.setdefault("layout", layout)
+        kw.setdefault("cull_mode", cull_mode)
+        return make_config(**kw)
+
+    def masks(self, full6: bool = False):
+        if self.isolated:
+            return [0] * len(self.coords)
+        return neighbour_masks(self.coords, full6)
+
+
+def workload(name: str) -> Workload:
+    """The synthetic workloads of the benchmark suite.
+
+    plain      8x8 chunks of 32^3 around the origin, 2-D Perlin heightmap (perm seed 42,
+               f = 1/64, amplitude 12, base 4)
+    heightmap  32x32 chunks of 16^3, 2-D fBm 4 octaves (lacunarity 2, gain 0.5,
+               f = 1/128), seed 7, amplitude 48, base 8
+    density    16x16x16 chunks of 32^3, 3-D fBm 3 octaves (f = 1/96, lacunarity 2,
+               gain 0.5), seed 1234, solid iff fbm - (y - 256)/64 > 0
+    stress     2048 isolated chunks of 64^3, Bernoulli(0.5) from splitmix64(99 ^ index)
+    """
+    if name == "plain":
+        return Workload(name, dict(chunk_size=32, kind=GEN_HEIGHTMAP, octaves=1, seed=42,
+                                   frequency=1.0 / 64, amplitude=12.0, base_height=4.0),
+                        tuple(grid_coords(range(-4, 4), [0], range(-4, 4))))
+    if name == "heightmap":
+        return Workload(name, dict(chunk_size=16, kind=GEN_HEIGHTMAP, octaves=4, seed=7,
+                                   frequency=1.0 / 128, lacunarity=2.0, gain=0.5, amplitude=48.0,
+                                   base_height=8.0),
+                        tuple(grid_coords(range(-16, 16), [0], range(-16, 16))))
+    if name == "density":
+        return Workload(name, dict(chunk_size=32, kind=GEN_DENSITY, octaves=3, seed=1234,
+                                   frequency=1.0 / 96, lacunarity=2.0, gain=0.5, y_ref=256.0,
+                                   y_scale=1.0 / 64),
+                        tuple(grid_coords(range(16), range(16), range(16))))
+    if name == "stress":
+        return Workload(name, dict(chunk_size=64, kind=GEN_BERNOULLI, seed=99),
+                        tuple((i, 0, 0) for i in range(2048)), isolated=True)
+    raise KeyError(name)
