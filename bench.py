@@ -57,6 +57,10 @@ def parse_args():
     p.add_argument("--e2e-steps", type=int, default=50)
     p.add_argument("--plain-steps", type=int, default=3)
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-autotune", action="store_true")
+    p.add_argument("--tuning", default=None,
+                   help="force a launch shape 'threads,stage_faces,ctas_per_sm' (no autotune)")
+    p.add_argument("--tune-iters", type=int, default=5)
     return p.parse_args()
 
 
@@ -261,6 +265,17 @@ def run_ours(args):
     o1 = torch.empty(cap * b1 + 16, dtype=torch.uint8, device="cuda") if b1 else None
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     total_faces = 0
+    # launch shape from the autotuner, timed on the first slab (setup, not timed)
+    tuning = None
+    if args.tuning:
+        th, st, cps = (int(v) for v in args.tuning.split(","))
+        ctx.set_tuning(th, st, cps)
+    elif not args.no_autotune:
+        a, b = slabs[0]
+        with torch.cuda.stream(stream):
+            tuning = ctx.autotune(d_coords[a:b], d_mask[a:b], b - a, o0, o1, cap, d_offs[a:b + 1],
+                                  chunk_index_base=wl.index_base + a, iters=args.tune_iters)
+    tuning = ctx.tuning().as_dict() | {"autotuned": tuning is not None}
 
     def step():
         for si, (a, b) in enumerate(slabs):
@@ -328,6 +343,7 @@ def run_ours(args):
         "config": {"workload": WORKLOAD_TEXT[args.workload], "chunks": n_all,
                    "chunk_size": cfg.chunk_size, "layout": args.layout,
                    "faces_per_step": total_faces, "launches_per_step": len(slabs),
+                   "tuning": tuning,
                    "l2": "flushed before every step (256 MiB write, outside the events)",
                    "parallelism": f"dp{world} (independent chunk batches)"},
         "voxels_per_s": value * cfg.chunk_size ** 3,

@@ -201,6 +201,34 @@ int vox_gen_mesh_host(vox_ctx* ctx, const vox_chunk_coord* h_coords, const uint8
                       int32_t n, int64_t chunk_index_base, void* h_out0, void* h_out1,
                       uint64_t cap_faces, uint64_t* h_face_offsets);
 
+/* ---- Tuning ------------------------------------------------------------------------------ */
+
+/* Launch shape of the meshing kernels. */
+typedef struct vox_tuning {
+  int32_t threads;     /* CTA size; each chunk size has two (8: 32/64, 16: 128/256,
+                          32: 256/512, 64: 512/1024) */
+  int32_t stage_faces; /* faces per shared-memory staging window (>= 6 * chunk_size), or 0 for
+                          direct global stores */
+  int32_t ctas_per_sm; /* resident CTAs per SM of the persistent grid; 0 = as many as fit */
+  int32_t reserved;
+} vox_tuning;
+
+int vox_ctx_get_tuning(vox_ctx* ctx, vox_tuning* out);
+int vox_ctx_set_tuning(vox_ctx* ctx, const vox_tuning* tuning);
+
+/* Autotuner: times every candidate launch shape (CTA size x staging window x CTAs per SM)
+ * on the given batch with vox_gen_mesh_batch (same arguments; iters launches each),
+ * keeps the fastest in the context and returns it in *out. The outputs of every
+ * candidate are identical; the buffers hold the last run's result. */
+int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
+                 int32_t n, int64_t chunk_index_base, void* d_out0, void* d_out1,
+                 uint64_t cap_faces, uint64_t* d_face_offsets, int32_t iters, vox_tuning* out);
+
+/* Self-test of the bounded device-side wait: runs one look-back whose predecessor never
+ * publishes. Returns VOX_ERR_TIMEOUT after spin_limit polls (no hang, no trap) and leaves
+ * the context usable. */
+int vox_selftest_lookback_timeout(vox_ctx* ctx, int32_t spin_limit);
+
 /* Page-locked host memory for the host-pointer entry points (cudaMallocHost). */
 int vox_host_alloc(size_t bytes, void** out);
 int vox_host_free(void* p);

@@ -316,3 +316,110 @@ def test_invalid_arguments_rejected(vox):
     with pytest.raises(vox.VoxError):  # misaligned vertex output
         ctx.gen_mesh_batch(d_coords, None, 2, bad.data_ptr() + 4, bad, 10, offs)
     ctx.close()
+
+
+def threads_options(n):
+    return {8: (32, 64), 16: (128, 256), 32: (256, 512), 64: (512, 1024)}[n]
+
+
+@pytest.mark.parametrize("wlname,sub,layout", [("heightmap", 160, 0), ("heightmap", 160, 1),
+                                               ("plain", 64, 0), ("stress", 2, 0),
+                                               ("stress", 2, 1)])
+def test_every_launch_shape_is_bit_exact(vox, oracle, wlname, sub, layout):
+    """CTA size, staging window (or direct stores) and CTAs per SM change only the speed."""
+    wl = vox.workload(wlname)
+    cfg = wl.config(layout=layout)
+    n = cfg.chunk_size
+    coords = list(wl.coords[:sub])
+    masks = None if wl.isolated else vox.neighbour_masks(coords)
+    w0, w1, woffs = oracle.gen_mesh_batch(cfg, coords, masks)
+    total = int(woffs[-1])
+    ctx = ctx_for(vox, cfg)
+    b0, b1 = ctx.sizes.bytes_per_face_out0, ctx.sizes.bytes_per_face_out1
+    d_coords = to_dev(np.asarray(coords, np.int32))
+    d_mask = None if masks is None else to_dev(np.asarray(masks, np.uint8))
+    o0, o1 = dev_bytes(total * b0), dev_bytes(max(total * b1, 16))
+    offs = to_dev(np.zeros(len(coords) + 1, np.uint64))
+    tried = 0
+    for threads in threads_options(n):
+        for stage in (0, 6 * n, 512, 2048):
+            for cps in (0, 2):
+                try:
+                    ctx.set_tuning(threads, stage, cps)
+                except vox.VoxError:
+                    continue  # the staging window does not fit in shared memory
+                o0.fill_(0x5A)
+                ctx.gen_mesh_batch(d_coords, d_mask, len(coords), o0, o1 if b1 else None, total, offs)
+                ctx.sync()
+                tag = (threads, stage, cps)
+                assert np.array_equal(to_np(offs), woffs), tag
+                assert np.array_equal(to_np(o0, total * b0), w0), tag
+                if b1:
+                    assert np.array_equal(to_np(o1, total * b1), w1), tag
+                tried += 1
+    assert tried >= 8
+    ctx.close()
+
+
+def test_autotune_picks_a_valid_shape(vox, oracle):
+    wl = vox.workload("heightmap")
+    cfg = wl.config()
+    coords = list(wl.coords)
+    masks = wl.masks()
+    w0, w1, woffs = oracle.gen_mesh_batch(cfg, coords, masks)
+    total = int(woffs[-1])
+    ctx = ctx_for(vox, cfg)
+    d_coords = to_dev(np.asarray(coords, np.int32))
+    d_mask = to_dev(np.asarray(masks, np.uint8))
+    o0, o1 = dev_bytes(total * 96), dev_bytes(total * 24)
+    offs = to_dev(np.zeros(len(coords) + 1, np.uint64))
+    t = ctx.autotune(d_coords, d_mask, len(coords), o0, o1, total, offs, iters=2)
+    assert t.threads in threads_options(16)
+    assert t.stage_faces == 0 or t.stage_faces >= 96
+    got = ctx.tuning()
+    assert (got.threads, got.stage_faces, got.ctas_per_sm) == (t.threads, t.stage_faces, t.ctas_per_sm)
+    o0.fill_(0)
+    ctx.gen_mesh_batch(d_coords, d_mask, len(coords), o0, o1, total, offs)
+    ctx.sync()
+    assert np.array_equal(to_np(o0, total * 96), w0) and np.array_equal(to_np(o1, total * 24), w1)
+    ctx.close()
+
+
+def test_bounded_wait_times_out_and_context_survives(vox, oracle):
+    """A look-back whose predecessor never publishes returns VOX_ERR_TIMEOUT (no hang, no
+    trap); the next batch on the same context is still exact."""
+    wl = vox.workload("plain")
+    cfg = wl.config()
+    ctx = ctx_for(vox, cfg)
+    assert ctx.selftest_lookback_timeout(2000) == vox.VOX_ERR_TIMEOUT
+    assert ctx.sync(raise_on_error=False) == vox.VOX_OK  # the error was reported once
+    coords = list(wl.coords[:8])
+    masks = vox.neighbour_masks(coords)
+    w0, w1, woffs = oracle.gen_mesh_batch(cfg, coords, masks)
+    total = int(woffs[-1])
+    d_coords = to_dev(np.asarray(coords, np.int32))
+    d_mask = to_dev(np.asarray(masks, np.uint8))
+    o0, o1 = dev_bytes(total * 96), dev_bytes(total * 24)
+    offs = to_dev(np.zeros(len(coords) + 1, np.uint64))
+    ctx.gen_mesh_batch(d_coords, d_mask, len(coords), o0, o1, total, offs)
+    ctx.sync()
+    assert np.array_equal(to_np(o0, total * 96), w0)
+    ctx.close()
+
+
+@pytest.mark.parametrize("stage", [0, 512])
+def test_single_chunk_direct_and_staged(vox, oracle, stage):
+    rng = np.random.default_rng(11)
+    cfg = vox.make_config(chunk_size=32)
+    cubes = np.where(rng.random(32 ** 3) < 0.5, 0, 2).astype(np.uint8)
+    w0, w1, wc = oracle.mesh_chunk(cfg, (3, -2, 5), cubes, [None] * 6)
+    ctx = ctx_for(vox, cfg)
+    ctx.set_tuning(512, stage, 0)
+    occ = to_dev(oracle.cubes_to_occ(32, cubes))
+    o0, o1 = dev_bytes(wc * 96), dev_bytes(wc * 24)
+    cnt = to_dev(np.zeros(1, np.uint64))
+    ctx.mesh(occ, [None] * 6, (3, -2, 5), o0, o1, wc, cnt)
+    ctx.sync()
+    assert int(to_np(cnt)[0]) == wc
+    assert np.array_equal(to_np(o0, wc * 96), w0) and np.array_equal(to_np(o1, wc * 24), w1)
+    ctx.close()

@@ -24,13 +24,18 @@ struct vox_ctx {
   vox_config cfg{};
   int device = 0;
   int num_sms = 0;
+  int max_smem_optin = 0;  // shared memory one block may opt in to
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   std::mutex mu;
   const KernelSet* ks = nullptr;
   GenDev gen{};
   int gm = GM_HEIGHT;
+  // tuning: CTA-size option, staging window (0 = direct stores), resident CTAs per SM
+  int topt = 0;
   int stage_faces = 0;
+  int ctas_per_sm = 0;
+  int spin_limit = kSpinLimit;
   int batch_grid[4] = {0, 0, 0, 0};  // persistent grid per gen mode
   TablesDev* d_tables = nullptr;
   BatchCtl* d_ctl = nullptr;
@@ -125,19 +130,52 @@ int gen_mode_of(int kind) {
   }
 }
 
-// Largest staging window that keeps two CTAs per SM (at least one full row: 6N faces).
+// Staging window of the default tuning: about 48 KB of shared memory per CTA (at least
+// one full row of faces, 6N).
 int default_stage_faces(const KernelSet& ks, int layout) {
-  const int budget = 100 * 1024;
-  const int per = layout == VOX_LAYOUT_INSTANCED ? 68 : 120;
-  int f = (budget - ks.smem_fixed[layout]) / per;
-  f = std::min(f, 4096);
-  f = std::max(f, 6 * ks.n_size);
+  const int budget = 48 * 1024;
+  int f = 6 * ks.n_size;
+  while (f + 32 <= 4096 && ks.smem_total(layout, ks.threads[0], f + 32) <= budget) f += 32;
   return f;
 }
 
+// Allows `fn` up to `smem` bytes of dynamic shared memory (capped at what the device
+// grants one block beyond the kernel's static shared memory).
 int prepare_kernel(vox_ctx* ctx, const void* fn, int smem) {
-  VOX_CUDA(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem),
+  cudaFuncAttributes fa;
+  VOX_CUDA(ctx, cudaFuncGetAttributes(&fa, fn), "cudaFuncGetAttributes");
+  const int limit = ctx->max_smem_optin - (int)fa.sharedSizeBytes;
+  VOX_CUDA(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     std::min(smem, limit)),
            "cudaFuncSetAttribute");
+  return VOX_OK;
+}
+
+// Validates a tuning and computes the persistent grid of every generator mode for it.
+int apply_tuning(vox_ctx* ctx, int topt, int stage_faces, int ctas_per_sm) {
+  const KernelSet& ks = *ctx->ks;
+  const int layout = ctx->cfg.layout;
+  if (topt < 0 || topt > 1) return fail(ctx, VOX_ERR_INVALID, "unsupported CTA size");
+  if (stage_faces != 0 && stage_faces < 6 * ks.n_size)
+    return fail(ctx, VOX_ERR_INVALID, "stage_faces must be 0 or at least 6 * chunk_size");
+  if (ctas_per_sm < 0) return fail(ctx, VOX_ERR_INVALID, "ctas_per_sm must be >= 0");
+  const int smem = ks.smem_total(layout, ks.threads[topt], stage_faces);
+  if (smem > ctx->max_smem_optin - 256)
+    return fail(ctx, VOX_ERR_INVALID, "staging window exceeds shared memory");
+  int grid[4];
+  for (int gm = 0; gm < 4; ++gm) {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+        &per_sm, ks.batch[gm][layout][topt], ks.threads[topt], smem);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+    if (per_sm < 1) return fail(ctx, VOX_ERR_INVALID, "kernel does not fit on an SM");
+    if (ctas_per_sm > 0) per_sm = std::min(per_sm, ctas_per_sm);
+    grid[gm] = per_sm * ctx->num_sms;
+  }
+  ctx->topt = topt;
+  ctx->stage_faces = stage_faces;
+  ctx->ctas_per_sm = ctas_per_sm;
+  for (int gm = 0; gm < 4; ++gm) ctx->batch_grid[gm] = grid[gm];
   return VOX_OK;
 }
 
@@ -174,12 +212,12 @@ MeshArgs base_args(vox_ctx* ctx) {
   a.gen = ctx->gen;
   a.full6 = ctx->cfg.cull_mode == VOX_CULL_FULL6 ? 1 : 0;
   a.stage_faces = ctx->stage_faces;
+  a.spin_limit = ctx->spin_limit;
   return a;
 }
 
-int launch(vox_ctx* ctx, const void* fn, int grid, int smem, void** params) {
-  VOX_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(ctx->ks->threads), params, (size_t)smem,
-                                 ctx->stream),
+int launch(vox_ctx* ctx, const void* fn, int grid, int threads, int smem, void** params) {
+  VOX_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(threads), params, (size_t)smem, ctx->stream),
            "cudaLaunchKernel");
   return VOX_OK;
 }
@@ -189,12 +227,13 @@ bool aligned(const void* p, size_t a) { return (reinterpret_cast<uintptr_t>(p) %
 int check_outputs(vox_ctx* ctx, void* out0, void* out1, uint64_t cap) {
   if (cap == 0) return VOX_OK;
   if (!out0) return fail(ctx, VOX_ERR_INVALID, "out0 is NULL with cap_faces > 0");
+  // Outputs are written with TMA bulk copies, which need 16-byte aligned addresses.
   if (ctx->cfg.layout == VOX_LAYOUT_VERTEX) {
     if (!out1) return fail(ctx, VOX_ERR_INVALID, "out1 (indices) is NULL with cap_faces > 0");
-    if (!aligned(out0, 16) || !aligned(out1, 8))
-      return fail(ctx, VOX_ERR_INVALID, "vertex output must be 16-byte aligned, indices 8-byte");
-  } else if (!aligned(out0, 4)) {
-    return fail(ctx, VOX_ERR_INVALID, "instance output must be 4-byte aligned");
+    if (!aligned(out0, 16) || !aligned(out1, 16))
+      return fail(ctx, VOX_ERR_INVALID, "vertex and index outputs must be 16-byte aligned");
+  } else if (!aligned(out0, 16)) {
+    return fail(ctx, VOX_ERR_INVALID, "instance output must be 16-byte aligned");
   }
   return VOX_OK;
 }
@@ -206,11 +245,11 @@ int batch_launch(vox_ctx* ctx, MeshArgs& a, int gm) {
   if (st != VOX_OK) return st;
   a.state = ctx->d_state;
   const int layout = ctx->cfg.layout;
-  const void* fn = ctx->ks->batch[gm][layout];
-  const int smem = ctx->ks->smem_total(layout, ctx->stage_faces);
+  const void* fn = ctx->ks->batch[gm][layout][ctx->topt];
+  const int smem = ctx->ks->smem_total(layout, ctx->ks->threads[ctx->topt], ctx->stage_faces);
   const int grid = std::max(1, std::min(a.n, ctx->batch_grid[gm]));
   void* params[] = {&a};
-  return launch(ctx, fn, grid, smem, params);
+  return launch(ctx, fn, grid, ctx->ks->threads[ctx->topt], smem, params);
 }
 
 }  // namespace
@@ -275,12 +314,16 @@ int vox_ctx_create(const vox_config* cfg, void* stream, vox_ctx** out) {
   ctx->gm = gen_mode_of(g.kind);
   int st = VOX_OK;
   auto cleanup = [&](int s) {
+    std::fprintf(stderr, "voxgpu: vox_ctx_create failed (%s): %s\n", vox_status_string(s),
+                 ctx->last_error.c_str());
     vox_ctx_destroy(ctx);
     return s;
   };
   if (cudaGetDevice(&ctx->device) != cudaSuccess) return cleanup(cuda_fail(ctx, cudaGetLastError(), "cudaGetDevice"));
-  if (cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess)
-    return cleanup(VOX_ERR_CUDA);
+  if (cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, ctx->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&ctx->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin,
+                             ctx->device) != cudaSuccess)
+    return cleanup(cuda_fail(ctx, cudaGetLastError(), "cudaDeviceGetAttribute"));
   if (stream) {
     ctx->stream = static_cast<cudaStream_t>(stream);
   } else {
@@ -296,22 +339,21 @@ int vox_ctx_create(const vox_config* cfg, void* stream, vox_ctx** out) {
   if (cudaMalloc(&ctx->d_ctl, sizeof(BatchCtl)) != cudaSuccess) return cleanup(VOX_ERR_OOM);
   if (cudaMemset(ctx->d_ctl, 0, sizeof(BatchCtl)) != cudaSuccess) return cleanup(VOX_ERR_CUDA);
   if (cudaMallocHost(&ctx->h_ctl, sizeof(BatchCtl)) != cudaSuccess) return cleanup(VOX_ERR_OOM);
-  ctx->stage_faces = default_stage_faces(*ctx->ks, cfg->layout);
-  // Kernel attributes and the persistent grid (resident CTAs per SM x SMs).
+  // Every meshing kernel may use up to the full shared memory of an SM; the tuning
+  // decides how much a launch actually takes.
   const int layout = cfg->layout;
-  const int smem = ctx->ks->smem_total(layout, ctx->stage_faces);
-  for (int gm = 0; gm < 4; ++gm) {
-    const void* fn = ctx->ks->batch[gm][layout];
-    if ((st = prepare_kernel(ctx, fn, smem)) != VOX_OK) return cleanup(st);
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, ctx->ks->threads, smem) != cudaSuccess || per_sm < 1)
-      return cleanup(fail(ctx, VOX_ERR_CUDA, "kernel does not fit on an SM"));
-    ctx->batch_grid[gm] = per_sm * ctx->num_sms;
-  }
-  if ((st = prepare_kernel(ctx, ctx->ks->single[layout], smem)) != VOX_OK) return cleanup(st);
-  const int gsmem = ctx->ks->smem_total(VOX_LAYOUT_VERTEX, 1);
+  for (int gm = 0; gm < 4; ++gm)
+    for (int t = 0; t < 2; ++t)
+      if ((st = prepare_kernel(ctx, ctx->ks->batch[gm][layout][t], ctx->max_smem_optin)) != VOX_OK)
+        return cleanup(st);
+  for (int t = 0; t < 2; ++t)
+    if ((st = prepare_kernel(ctx, ctx->ks->single[layout][t], ctx->max_smem_optin)) != VOX_OK)
+      return cleanup(st);
+  const int gsmem = ctx->ks->smem_total(VOX_LAYOUT_VERTEX, ctx->ks->gen_threads, 0);
   for (int gm = 1; gm < 4; ++gm)
     if ((st = prepare_kernel(ctx, ctx->ks->generate[gm], gsmem)) != VOX_OK) return cleanup(st);
+  if ((st = apply_tuning(ctx, 0, default_stage_faces(*ctx->ks, layout), 0)) != VOX_OK)
+    return cleanup(st);
   if ((st = ensure_state(ctx, 1024)) != VOX_OK) return cleanup(st);
   if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return cleanup(VOX_ERR_CUDA);
   *out = ctx;
@@ -371,8 +413,8 @@ int vox_generate(vox_ctx* ctx, const vox_chunk_coord* d_coords, int32_t n,
   a.coords = d_coords;
   uint32_t* occ = d_occ;
   void* params[] = {&a, &occ};
-  return launch(ctx, ctx->ks->generate[ctx->gm], n, ctx->ks->smem_total(VOX_LAYOUT_VERTEX, 1),
-                params);
+  return launch(ctx, ctx->ks->generate[ctx->gm], n, ctx->ks->gen_threads,
+                ctx->ks->smem_total(VOX_LAYOUT_VERTEX, ctx->ks->gen_threads, 0), params);
 }
 
 int vox_occ_to_cubes(vox_ctx* ctx, const uint32_t* d_occ, int32_t n, uint8_t* d_cubes) {
@@ -412,7 +454,8 @@ int vox_mesh(vox_ctx* ctx, const uint32_t* d_occ, const uint32_t* const d_nbr[6]
   a.face_offsets = reinterpret_cast<unsigned long long*>(d_face_count);
   void* params[] = {&a};
   const int layout = ctx->cfg.layout;
-  return launch(ctx, ctx->ks->single[layout], 1, ctx->ks->smem_total(layout, ctx->stage_faces),
+  return launch(ctx, ctx->ks->single[layout][ctx->topt], 1, ctx->ks->threads[ctx->topt],
+                ctx->ks->smem_total(layout, ctx->ks->threads[ctx->topt], ctx->stage_faces),
                 params);
 }
 
@@ -572,6 +615,112 @@ int vox_frustum_cull(vox_ctx* ctx, const float planes[24], const vox_chunk_coord
   VOX_CUDA(ctx, launch_frustum(pl, d_coords, n, ctx->cfg.chunk_size, d_visible, ctx->stream),
            "frustum");
   return VOX_OK;
+}
+
+int vox_ctx_get_tuning(vox_ctx* ctx, vox_tuning* out) {
+  if (!ctx || !out) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  out->threads = ctx->ks->threads[ctx->topt];
+  out->stage_faces = ctx->stage_faces;
+  out->ctas_per_sm = ctx->ctas_per_sm;
+  out->reserved = 0;
+  return VOX_OK;
+}
+
+int vox_ctx_set_tuning(vox_ctx* ctx, const vox_tuning* t) {
+  if (!ctx || !t) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  int topt = -1;
+  for (int k = 0; k < 2; ++k)
+    if (ctx->ks->threads[k] == t->threads) topt = k;
+  if (topt < 0) return fail(ctx, VOX_ERR_INVALID, "threads must be %d or %d", ctx->ks->threads[0],
+                            ctx->ks->threads[1]);
+  return apply_tuning(ctx, topt, t->stage_faces, t->ctas_per_sm);
+}
+
+int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
+                 int32_t n, int64_t chunk_index_base, void* d_out0, void* d_out1,
+                 uint64_t cap_faces, uint64_t* d_face_offsets, int32_t iters, vox_tuning* out) {
+  if (!ctx) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (n <= 0 || !d_coords || !d_face_offsets || iters < 1)
+    return fail(ctx, VOX_ERR_INVALID, "bad arguments");
+  int st = check_outputs(ctx, d_out0, d_out1, cap_faces);
+  if (st != VOX_OK) return st;
+  const int N = ctx->cfg.chunk_size;
+  const int stages[] = {0, 6 * N, 256, 512, 1024, 2048, 4096};
+  const int ctas[] = {0, 4, 2};
+  cudaEvent_t e0, e1;
+  VOX_CUDA(ctx, cudaEventCreate(&e0), "cudaEventCreate");
+  VOX_CUDA(ctx, cudaEventCreate(&e1), "cudaEventCreate");
+  const int keep_t = ctx->topt, keep_s = ctx->stage_faces, keep_c = ctx->ctas_per_sm;
+  float best_ms = 1e30f;
+  int best_t = keep_t, best_s = keep_s, best_c = keep_c;
+  auto run = [&]() {
+    MeshArgs a = base_args(ctx);
+    a.n = n;
+    a.index_base = chunk_index_base;
+    a.coords = d_coords;
+    a.nbr_mask = d_nbr_mask;
+    a.out0 = d_out0;
+    a.out1 = d_out1;
+    a.cap = cap_faces;
+    a.face_offsets = reinterpret_cast<unsigned long long*>(d_face_offsets);
+    return batch_launch(ctx, a, ctx->gm);
+  };
+  for (int t = 0; t < 2 && st == VOX_OK; ++t)
+    for (int s : stages) {
+      if (s != 0 && s < 6 * N) continue;
+      int full_grid = 0;
+      for (int c : ctas) {
+        if (apply_tuning(ctx, t, s, c) != VOX_OK) continue;
+        if (c == 0) full_grid = ctx->batch_grid[ctx->gm];
+        else if (ctx->batch_grid[ctx->gm] >= full_grid) continue;  // same grid as c = 0
+        if ((st = run()) != VOX_OK) break;
+        cudaEventRecord(e0, ctx->stream);
+        for (int k = 0; k < iters && st == VOX_OK; ++k) st = run();
+        cudaEventRecord(e1, ctx->stream);
+        if (st != VOX_OK) break;
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+          st = cuda_fail(ctx, cudaGetLastError(), "autotune");
+          break;
+        }
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_ms) {
+          best_ms = ms;
+          best_t = t;
+          best_s = s;
+          best_c = c;
+        }
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->last_error.clear();
+  const int st2 = apply_tuning(ctx, best_t, best_s, best_c);
+  if (st == VOX_OK) st = st2;
+  if (st == VOX_OK) st = sync_locked(ctx);
+  if (st != VOX_OK) apply_tuning(ctx, keep_t, keep_s, keep_c);
+  if (out) {
+    out->threads = ctx->ks->threads[ctx->topt];
+    out->stage_faces = ctx->stage_faces;
+    out->ctas_per_sm = ctx->ctas_per_sm;
+    out->reserved = 0;
+  }
+  return st;
+}
+
+int vox_selftest_lookback_timeout(vox_ctx* ctx, int32_t spin_limit) {
+  if (!ctx || spin_limit < 1) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  unsigned long long* words = nullptr;
+  VOX_CUDA(ctx, cudaMalloc(&words, 2 * sizeof(unsigned long long)), "cudaMalloc(probe)");
+  cudaError_t e = cudaMemsetAsync(words, 0, 2 * sizeof(unsigned long long), ctx->stream);
+  if (e == cudaSuccess) e = launch_lookback_probe(words, ctx->d_ctl, spin_limit, ctx->stream);
+  const int st = e == cudaSuccess ? sync_locked(ctx) : cuda_fail(ctx, e, "lookback probe");
+  cudaFree(words);
+  return st;
 }
 
 int vox_host_alloc(size_t bytes, void** out) {

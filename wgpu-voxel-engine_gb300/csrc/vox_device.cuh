@@ -3,10 +3,11 @@
 // One CTA owns one chunk at a time. The chunk's occupancy lives in shared memory as
 // one N-bit row per (y, z) (bit x = voxel solid), plus six halo rows per side. Face
 // masks of a row come from shifts of the row and its neighbours, counts from popc.
-// A deterministic block scan over rows gives every row's first face; chunks of a
-// batch get their global first face from a decoupled look-back over a device work
-// queue. Faces are written voxel-parallel into a shared-memory staging window in the
-// final byte layout and copied out with coalesced stores.
+// A deterministic block scan over rows gives every row's first face and a compacted
+// list of the rows that have faces; chunks of a batch get their global first face from
+// a decoupled look-back over a device work queue. Faces are written voxel-parallel into
+// a shared-memory staging window in their final byte layout, and the window goes to
+// global memory with TMA bulk copies (cp.async.bulk.global.shared::cta).
 //
 // Reference semantics restated here (Blatko1/wgpu-voxel-engine):
 //   fill rule            src/chunk.rs:35-45     (solid -> GRASS, else AIR)
@@ -32,14 +33,30 @@ struct Shape {
   using RowT = typename std::conditional<(N > 32), unsigned long long, uint32_t>::type;
   static constexpr int R = N * N;                 // rows per chunk
   static constexpr int W = N > 32 ? N / 32 : 1;   // u32 words per row
-  static constexpr int THREADS = N == 64 ? 512 : (N == 8 ? 64 : 256);
-  static constexpr int RPT = R / THREADS;         // rows per thread in the scan
-  static constexpr int LPR = N < 32 ? N : 32;     // lanes per row segment
+  // CTA sizes the kernels are instantiated for (rows split evenly over the threads)
+  static constexpr int T0 = N == 8 ? 32 : (N == 16 ? 128 : (N == 32 ? 256 : 512));
+  static constexpr int T1 = 2 * T0;
 };
 
 __host__ __device__ constexpr int align16(int b) { return (b + 15) & ~15; }
 
-// Shared-memory carve-up; the same function sizes the launch on the host.
+// Per-octave lattice data of one column coordinate (heightmap generation).
+struct AxisX {
+  int px, px1;  // p[X], p[X + 1]
+  float fr, u;  // fractional coordinate and its fade
+};
+struct AxisZ {
+  int y;        // lattice Y & 255
+  float fr, v;  // fractional coordinate and its fade
+  int pad;
+};
+
+// Octaves whose per-axis lattice data are computed between one pair of barriers.
+constexpr int kOctGroup = 8;
+// Faces one warp's 32 voxels can have (6 each): the size of a warp's face list.
+constexpr int kWarpFaces = 32 * 6;
+
+// Shared-memory carve-up; the same functions size the launch on the host.
 template <int N, int LAYOUT>
 struct SmemPlan {
   using RowT = typename Shape<N>::RowT;
@@ -47,14 +64,26 @@ struct SmemPlan {
   static constexpr int kOcc = align16(Shape<N>::R * (int)sizeof(RowT));
   static constexpr int kHalo = align16(6 * N * (int)sizeof(RowT));
   static constexpr int kRows = align16((Shape<N>::R + 1) * 4);
+  static constexpr int kNz = align16(Shape<N>::R * 2);
   static constexpr int kMisc = 64;
+  static constexpr int kFixed0 = kTables + kOcc + kHalo + kRows + kNz + kMisc;
+  // per-warp face lists (face-parallel emission)
+  __host__ __device__ static int list_bytes(int threads) { return (threads / 32) * kWarpFaces * 4; }
+  __host__ __device__ static int fixed(int threads) { return kFixed0 + list_bytes(threads); }
+  // generation scratch, aliased with the staging window
   static constexpr int kColK = align16((N + 2) * (N + 2) * 4);
-  static constexpr int kFixed = kTables + kOcc + kHalo + kRows + kMisc;
+  static constexpr int kAxisHalf = kOctGroup * align16((N + 2) * 16);
+  static constexpr int kAxis = 2 * kAxisHalf;
+  static constexpr int kZRange = align16(2 * N * 4);
+  static constexpr int kGenScratch = kColK + kAxis + kZRange;
   __host__ __device__ static int stage_bytes(int faces) {
-    int b = LAYOUT == VOX_LAYOUT_INSTANCED ? align16(faces * 68) : faces * 96 + align16(faces * 24);
-    return b < kColK ? kColK : b;
+    int b = LAYOUT == VOX_LAYOUT_INSTANCED ? align16(faces * 68 + 16)
+                                           : faces * 96 + align16(faces * 24 + 16);
+    return b < kGenScratch ? kGenScratch : b;
   }
-  __host__ __device__ static int total(int faces) { return kFixed + stage_bytes(faces); }
+  __host__ __device__ static int total(int threads, int faces) {
+    return fixed(threads) + stage_bytes(faces);
+  }
 };
 
 // ------------------------------------------------------------------------------------
@@ -95,27 +124,15 @@ __device__ __forceinline__ float d_noise3(const uint8_t* p, float x, float y, fl
   return d_lerp(w, d_lerp(v, l00, l10), d_lerp(v, l01, l11));
 }
 
-__device__ __forceinline__ float d_noise2(const uint8_t* p, float x, float y) {
-  float fx = floorf(x), fy = floorf(y);
-  int X = (int)fx & 255, Y = (int)fy & 255;
-  x = x - fx;
-  y = y - fy;
-  float u = d_fade(x), v = d_fade(y);
-  int A = p[X] + Y, B = p[X + 1] + Y;
-  float x1 = x - 1.0f, y1 = y - 1.0f;
-  float l0 = d_lerp(u, d_grad2(p[p[A]], x, y), d_grad2(p[p[B]], x1, y));
-  float l1 = d_lerp(u, d_grad2(p[p[A + 1]], x, y1), d_grad2(p[p[B + 1]], x1, y1));
-  return d_lerp(v, l0, l1);
-}
-
-__device__ __forceinline__ float d_fbm2(const uint8_t* p, float x, float y, const GenDev& g) {
-  float sum = 0.0f, amp = 1.0f, f = g.freq;
-  for (int o = 0; o < g.octaves; ++o) {
-    sum = sum + amp * d_noise2(p, x * f, y * f);
-    f = f * g.lac;
-    amp = amp * g.gain;
-  }
-  return sum;
+// noise2 at a column whose per-axis lattice data were computed once per octave; the
+// operations are those of the oracle's or_noise2_f32, minus the shared subexpressions.
+__device__ __forceinline__ float d_noise2_axes(const uint8_t* p, const AxisX& ax, const AxisZ& az) {
+  const int A = ax.px + az.y, B = ax.px1 + az.y;
+  const float x = ax.fr, y = az.fr;
+  const float x1 = x - 1.0f, y1 = y - 1.0f;
+  const float l0 = d_lerp(ax.u, d_grad2(p[p[A]], x, y), d_grad2(p[p[B]], x1, y));
+  const float l1 = d_lerp(ax.u, d_grad2(p[p[A + 1]], x, y1), d_grad2(p[p[B + 1]], x1, y1));
+  return d_lerp(az.v, l0, l1);
 }
 
 __device__ __forceinline__ float d_fbm3(const uint8_t* p, float x, float y, float z,
@@ -159,6 +176,36 @@ __device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned* p) {
   return v;
 }
 
+// TMA bulk copies shared -> global (cp.async.bulk, bulk-group completion).
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_s2g(void* gdst, const void* ssrc, uint32_t bytes) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(ssrc);
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+               ::"l"(gdst), "r"(s), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_read_all() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+// Issues [src, src + bytes) -> dst in pieces of at most 32 KiB (16-byte multiples).
+__device__ __forceinline__ void bulk_s2g_pieces(unsigned char* dst, const unsigned char* src,
+                                                uint32_t bytes) {
+  while (bytes > 0) {
+    const uint32_t b = bytes > 32768u ? 32768u : bytes;
+    bulk_s2g(dst, src, b);
+    dst += b;
+    src += b;
+    bytes -= b;
+  }
+}
+
 // Look-back state word: epoch (24 bits) | flag (2 bits) | value (38 bits).
 constexpr unsigned long long kFlagAgg = 1ull;
 constexpr unsigned long long kFlagIncl = 2ull;
@@ -179,20 +226,40 @@ struct ChunkSmem {
   RowT* occ;        // [R]
   RowT* halo;       // [6][N]: 0 -x (bits z, by y), 1 +x, 2 -z (bits x, by y), 3 +z, 4 -y (bits x, by z), 5 +y
   uint32_t* rows;   // [R + 1] exclusive face offsets per row
-  long long* misc;  // broadcast slots
+  uint16_t* nz;     // rows that have faces, ascending
+  int* misc;        // [0] rows with faces; [1..3] current window (k1, f0, nf)
+  uint32_t* lists;  // per-warp face lists (packed x, y, z, dir)
   unsigned char* stage;
-  int* colk;        // heightmap column thresholds, aliased with stage
+  // generation scratch (aliased with the staging window)
+  int* colk;        // heightmap column thresholds
+  AxisX* ax;        // per-octave x-axis lattice data, [kOctGroup][N + 2]
+  AxisZ* az;        // per-octave z-axis lattice data, [kOctGroup][N + 2]
+  int* zmin;        // per z: min / max column threshold over x
+  int* zmax;
 
-  __device__ void carve(unsigned char* base, int stage_faces) {
+  __device__ void carve(unsigned char* base) {
     using P = SmemPlan<N, LAYOUT>;
-    tab = reinterpret_cast<TablesDev*>(base);
-    occ = reinterpret_cast<RowT*>(base + P::kTables);
-    halo = reinterpret_cast<RowT*>(base + P::kTables + P::kOcc);
-    rows = reinterpret_cast<uint32_t*>(base + P::kTables + P::kOcc + P::kHalo);
-    misc = reinterpret_cast<long long*>(base + P::kTables + P::kOcc + P::kHalo + P::kRows);
-    stage = base + P::kFixed;
-    colk = reinterpret_cast<int*>(stage);
-    (void)stage_faces;
+    unsigned char* q = base;
+    tab = reinterpret_cast<TablesDev*>(q);
+    q += P::kTables;
+    occ = reinterpret_cast<RowT*>(q);
+    q += P::kOcc;
+    halo = reinterpret_cast<RowT*>(q);
+    q += P::kHalo;
+    rows = reinterpret_cast<uint32_t*>(q);
+    q += P::kRows;
+    nz = reinterpret_cast<uint16_t*>(q);
+    q += P::kNz;
+    misc = reinterpret_cast<int*>(q);
+    q += P::kMisc;
+    lists = reinterpret_cast<uint32_t*>(q);
+    q += P::list_bytes(blockDim.x);
+    stage = q;
+    colk = reinterpret_cast<int*>(q);
+    ax = reinterpret_cast<AxisX*>(q + P::kColK);
+    az = reinterpret_cast<AxisZ*>(q + P::kColK + P::kAxisHalf);
+    zmin = reinterpret_cast<int*>(q + P::kColK + P::kAxis);
+    zmax = zmin + N;
   }
 };
 
@@ -218,6 +285,12 @@ __device__ __forceinline__ void store_ballot(uint32_t* words, int e, bool pred) 
   }
 }
 
+template <int N>
+__device__ __forceinline__ typename Shape<N>::RowT full_row() {
+  using RowT = typename Shape<N>::RowT;
+  return N >= 64 ? (RowT)~0ull : (RowT)((1ull << (N & 63)) - 1ull);
+}
+
 // ------------------------------------------------------------------------------------
 // Occupancy generation into shared memory
 // ------------------------------------------------------------------------------------
@@ -235,34 +308,130 @@ __device__ __forceinline__ void halo_coord(int h, int a, int b, int& x, int& y, 
   }
 }
 
-// Heightmap: colk[(z+1)*(N+2) + (x+1)] = ceil(h(x, z)) - oy clamped to [-1, N + 1], so
-// voxel (x, y, z) with y in [-1, N] is solid iff y < colk (== (float)(oy + y) < h).
-template <int N, int LAYOUT>
-__device__ void height_columns(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, int oy, int oz) {
-  const int side = N + 2;
-  for (int i = threadIdx.x; i < side * side; i += blockDim.x) {
-    const int zz = i / side - 1, xx = i % side - 1;
-    const bool corner = (zz < 0 || zz >= N) && (xx < 0 || xx >= N);
-    int k = 0;
-    if (!corner) {
-      const float f = d_fbm2(s.tab->perm, (float)(ox + xx), (float)(oz + zz), g);
-      const float h = g.base + g.amp * f;
-      const float c = ceilf(h);
-      long long kk = (long long)c - (long long)oy;
-      if (!(c == c)) kk = -1;  // NaN cannot occur for finite inputs; keep it air
-      k = (int)(kk < -1 ? -1 : (kk > N + 1 ? N + 1 : kk));
+// Heightmap chunk. Column thresholds colk[(z+1)*(N+2) + (x+1)] = ceil(h(x, z)) - oy,
+// clamped to [-1, N + 1], so that voxel (x, y, z), y in [-1, N], is solid iff
+// y < colk (the same as (float)(oy + y) < h for the integer y). The fBm runs octave by
+// octave: the lattice data of every x and z coordinate are computed once per octave,
+// each thread accumulating its own columns in registers.
+template <int N, int LAYOUT, int T>
+__device__ void gen_heightmap(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, int oy, int oz,
+                              unsigned halo_mask, bool with_halo) {
+  using RowT = typename Shape<N>::RowT;
+  constexpr int side = N + 2;
+  constexpr int CPT = (side * side + T - 1) / T;
+  const int t = threadIdx.x;
+  const uint8_t* p = s.tab->perm;
+  float acc[CPT];
+#pragma unroll
+  for (int c = 0; c < CPT; ++c) acc[c] = 0.0f;
+  float f = g.freq, amp = 1.0f;
+  for (int o0 = 0; o0 < g.octaves; o0 += kOctGroup) {
+    const int no = g.octaves - o0 < kOctGroup ? g.octaves - o0 : kOctGroup;
+    // lattice data of every x and z coordinate for the octaves [o0, o0 + no)
+    for (int i = t; i < 2 * side * no; i += T) {
+      const int o = i / (2 * side), r = i % (2 * side);
+      const int a = r / side, k = r % side - 1;
+      float fo = f;
+      for (int q = 0; q < o; ++q) fo = fo * g.lac;
+      const float c = (float)(a == 0 ? ox + k : oz + k) * fo;
+      const float fl = floorf(c);
+      const int L = (int)fl & 255;
+      const float fr = c - fl;
+      if (a == 0) {
+        AxisX v;
+        v.px = p[L];
+        v.px1 = p[L + 1];
+        v.fr = fr;
+        v.u = d_fade(fr);
+        s.ax[o * side + k + 1] = v;
+      } else {
+        AxisZ v;
+        v.y = L;
+        v.fr = fr;
+        v.v = d_fade(fr);
+        v.pad = 0;
+        s.az[o * side + k + 1] = v;
+      }
     }
-    s.colk[i] = k;
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) {
+      const int j = t + c * T;
+      if (j < side * side) {
+        const int zi = j / side, xi = j % side;
+        const bool corner = (zi == 0 || zi == side - 1) && (xi == 0 || xi == side - 1);
+        if (!corner) {
+          float a = amp, sum = acc[c];
+          for (int o = 0; o < no; ++o) {
+            sum = sum + a * d_noise2_axes(p, s.ax[o * side + xi], s.az[o * side + zi]);
+            a = a * g.gain;
+          }
+          acc[c] = sum;
+        }
+      }
+    }
+    for (int o = 0; o < no; ++o) {
+      f = f * g.lac;
+      amp = amp * g.gain;
+    }
+    __syncthreads();
   }
+#pragma unroll
+  for (int c = 0; c < CPT; ++c) {
+    const int j = t + c * T;
+    if (j < side * side) {
+      const float h = g.base + g.amp * acc[c];
+      const float cl = ceilf(h);
+      long long kk = (long long)cl - (long long)oy;
+      if (!(cl == cl)) kk = -1;
+      s.colk[j] = (int)(kk < -1 ? -1 : (kk > N + 1 ? N + 1 : kk));
+    }
+  }
+  __syncthreads();
+  for (int z = t; z < N; z += T) {
+    int mn = N + 1, mx = -1;
+    for (int x = 0; x < N; ++x) {
+      const int k = s.colk[(z + 1) * side + x + 1];
+      mn = k < mn ? k : mn;
+      mx = k > mx ? k : mx;
+    }
+    s.zmin[z] = mn;
+    s.zmax[z] = mx;
+  }
+  __syncthreads();
+  for (int r = t; r < N * N; r += T) {
+    const int y = r / N, z = r % N;
+    RowT row = 0;
+    if (y < s.zmin[z]) {
+      row = full_row<N>();
+    } else if (y < s.zmax[z]) {
+      const int* kz = s.colk + (z + 1) * side + 1;
+      for (int x = 0; x < N; ++x) row |= (RowT)(y < kz[x] ? 1u : 0u) << x;
+    }
+    s.occ[r] = row;
+  }
+  if (with_halo) {
+    for (int i = t; i < 6 * N; i += T) {
+      const int h = i / N, a = i % N;
+      RowT row = 0;
+      if ((halo_mask >> h) & 1u) {
+        for (int b = 0; b < N; ++b) {
+          int x, y, z;
+          halo_coord<N>(h, a, b, x, y, z);
+          row |= (RowT)(y < s.colk[(z + 1) * side + x + 1] ? 1u : 0u) << b;
+        }
+      }
+      s.halo[i] = row;
+    }
+  }
+  __syncthreads();
 }
 
 template <int N, int GM, int LAYOUT>
 __device__ __forceinline__ bool gen_solid(const ChunkSmem<N, LAYOUT>& s, const GenDev& g, int x,
                                           int y, int z, int ox, int oy, int oz,
                                           unsigned long long s0) {
-  if (GM == GM_HEIGHT) {
-    return y < s.colk[(z + 1) * (N + 2) + (x + 1)];
-  } else if (GM == GM_DENSITY) {
+  if (GM == GM_DENSITY) {
     const int wy = oy + y;
     const float f = d_fbm3(s.tab->perm, (float)(ox + x), (float)wy, (float)(oz + z), g);
     const float d = f - ((float)wy - g.y_ref) * g.y_scale;
@@ -275,16 +444,16 @@ __device__ __forceinline__ bool gen_solid(const ChunkSmem<N, LAYOUT>& s, const G
 
 // Fills s.occ (own rows) and, for every set bit of `halo_mask`, the halo rows; the other
 // halo rows are zero (a neighbour that is not loaded counts as air, chunk.rs:102-107).
-template <int N, int GM, int LAYOUT>
+template <int N, int GM, int LAYOUT, int T>
 __device__ void gen_chunk(ChunkSmem<N, LAYOUT>& s, const GenDev& g, vox_chunk_coord c,
                           long long chunk_index, unsigned halo_mask, bool with_halo) {
   using RowT = typename Shape<N>::RowT;
   const int ox = c.x * N, oy = c.y * N, oz = c.z * N;
-  const unsigned long long s0 = g.seed ^ (unsigned long long)chunk_index;
   if (GM == GM_HEIGHT) {
-    height_columns<N, LAYOUT>(s, g, ox, oy, oz);
-    __syncthreads();
+    gen_heightmap<N, LAYOUT, T>(s, g, ox, oy, oz, halo_mask, with_halo);
+    return;
   }
+  const unsigned long long s0 = g.seed ^ (unsigned long long)chunk_index;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   uint32_t* occw = reinterpret_cast<uint32_t*>(s.occ);
   for (int base = warp * 32; base < N * N * N; base += nwarps * 32) {
@@ -379,14 +548,16 @@ __device__ __forceinline__ void row_masks(const ChunkSmem<N, LAYOUT>& s, int y, 
   m[5] = row & ~un;
 }
 
-// Per-row face counts -> exclusive offsets in s.rows[0..R]; returns the chunk total.
-template <int N, int LAYOUT>
+// Per-row face counts -> exclusive offsets in s.rows[0..R] and the ascending list of the
+// rows with faces in s.nz (count in s.misc[0]); returns the chunk's face total.
+template <int N, int LAYOUT, int T>
 __device__ uint32_t count_and_scan(ChunkSmem<N, LAYOUT>& s) {
   using RowT = typename Shape<N>::RowT;
-  constexpr int RPT = Shape<N>::RPT;
+  constexpr int RPT = Shape<N>::R / T;
+  static_assert(RPT >= 1 && RPT * T == Shape<N>::R, "rows must split evenly over threads");
   const int t = threadIdx.x;
   uint32_t cnt[RPT];
-  uint32_t local = 0;
+  uint32_t local = 0, nzl = 0;
 #pragma unroll
   for (int k = 0; k < RPT; ++k) {
     const int r = t * RPT + k;
@@ -397,46 +568,61 @@ __device__ uint32_t count_and_scan(ChunkSmem<N, LAYOUT>& s) {
     for (int d = 0; d < 6; ++d) c += (uint32_t)popc_row(m[d]);
     cnt[k] = c;
     local += c;
+    nzl += c != 0u ? 1u : 0u;
   }
-  // Deterministic block scan: warp inclusive scan, then a scan of the warp totals.
-  const int lane = t & 31, warp = t >> 5, nwarps = blockDim.x >> 5;
-  uint32_t incl = local;
+  // Deterministic block scan of (faces << 16 | rows with faces): warp inclusive scan,
+  // then a scan of the warp totals.
+  const int lane = t & 31, warp = t >> 5, nwarps = T >> 5;
+  const unsigned long long mine = ((unsigned long long)local << 16) | nzl;
+  unsigned long long incl = mine;
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
-    const uint32_t v = __shfl_up_sync(0xffffffffu, incl, off);
+    const unsigned long long v = __shfl_up_sync(0xffffffffu, incl, off);
     if (lane >= off) incl += v;
   }
-  uint32_t* wsum = reinterpret_cast<uint32_t*>(s.stage);  // scratch: staging is free here
+  unsigned long long* wsum = reinterpret_cast<unsigned long long*>(s.stage);  // staging is free
   if (lane == 31) wsum[warp] = incl;
   __syncthreads();
   if (warp == 0) {
-    uint32_t v = lane < nwarps ? wsum[lane] : 0u;
-    uint32_t vi = v;
+    const unsigned long long v = lane < nwarps ? wsum[lane] : 0ull;
+    unsigned long long vi = v;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
-      const uint32_t u = __shfl_up_sync(0xffffffffu, vi, off);
+      const unsigned long long u = __shfl_up_sync(0xffffffffu, vi, off);
       if (lane >= off) vi += u;
     }
     if (lane < nwarps) wsum[32 + lane] = vi - v;  // exclusive warp offsets
-    if (lane == nwarps - 1) wsum[64] = vi;         // chunk total
+    if (lane == nwarps - 1) wsum[64] = vi;         // chunk totals
   }
   __syncthreads();
-  uint32_t run = wsum[32 + warp] + incl - local;
+  const unsigned long long excl = wsum[32 + warp] + incl - mine;
+  uint32_t run = (uint32_t)(excl >> 16);
+  uint32_t nzrun = (uint32_t)(excl & 0xFFFFu);
 #pragma unroll
   for (int k = 0; k < RPT; ++k) {
-    s.rows[t * RPT + k] = run;
+    const int r = t * RPT + k;
+    s.rows[r] = run;
+    if (cnt[k] != 0u) s.nz[nzrun++] = (uint16_t)r;
     run += cnt[k];
   }
-  const uint32_t total = wsum[64];
-  if (t == 0) s.rows[Shape<N>::R] = total;
+  const unsigned long long tot = wsum[64];
+  const uint32_t total = (uint32_t)(tot >> 16);
+  if (t == 0) {
+    s.rows[Shape<N>::R] = total;
+    s.misc[0] = (int)(tot & 0xFFFFu);
+  }
   __syncthreads();
   return total;
 }
 
 // Decoupled look-back over chunks (warp 0 of the CTA). Returns the exclusive prefix of
-// chunk i. Every wait is bounded; on timeout the error bit is set and 0 is used.
-static __device__ unsigned long long lookback(unsigned long long* state, BatchCtl* ctl, unsigned epoch,
-                                       int i, unsigned long long total) {
+// chunk i. Each poll reads a window of 128 predecessors (4 per lane, coalesced), walks
+// back to the nearest inclusive prefix and sums the aggregates in between. Every wait is
+// bounded (spin_limit polls); on timeout the error bit is set and 0 is used.
+constexpr int kLookbackWindow = 128;
+static __device__ unsigned long long lookback(unsigned long long* state, BatchCtl* ctl,
+                                              unsigned epoch, int i, unsigned long long total,
+                                              int spin_limit) {
   const int lane = threadIdx.x & 31;
   unsigned long long excl = 0;
   if (i == 0) {
@@ -444,46 +630,80 @@ static __device__ unsigned long long lookback(unsigned long long* state, BatchCt
     return 0;
   }
   if (lane == 0) st_relaxed_u64(&state[i], pack_state(epoch, kFlagAgg, total));
+  const unsigned tag = epoch & 0xFFFFFFu;
+  const unsigned long long vmask = (1ull << 38) - 1;
   int j = i - 1;
   int spins = 0;
-  unsigned sleep_ns = 32;
   while (true) {
-    const int idx = j - lane;
-    unsigned long long sv = idx >= 0 ? ld_relaxed_u64(&state[idx]) : pack_state(epoch, kFlagIncl, 0);
-    const unsigned e = (unsigned)(sv >> 40) & 0xFFFFFFu;
-    const unsigned long long flag = (sv >> 38) & 3ull;
-    const bool valid = (e == (epoch & 0xFFFFFFu)) && flag != 0ull;
-    const unsigned incl_mask = __ballot_sync(0xffffffffu, valid && flag == kFlagIncl);
-    const unsigned bad_mask = __ballot_sync(0xffffffffu, !valid);
-    const int first_incl = incl_mask ? __ffs(incl_mask) - 1 : 32;
-    const unsigned need = first_incl >= 31 ? 0xffffffffu : ((2u << first_incl) - 1u);
-    if (bad_mask & need) {
-      if (++spins > kSpinLimit) {
+    // window position p = 32k + lane <-> chunk j - p (p = 0 is the nearest predecessor)
+    unsigned long long sv[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int idx = j - (32 * k + lane);
+      sv[k] = idx >= 0 ? ld_relaxed_u64(&state[idx]) : pack_state(epoch, kFlagIncl, 0);
+    }
+    int first_incl = kLookbackWindow;
+    unsigned bad[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const unsigned e = (unsigned)(sv[k] >> 40) & 0xFFFFFFu;
+      const unsigned long long flag = (sv[k] >> 38) & 3ull;
+      const bool valid = e == tag && flag != 0ull;
+      const unsigned incl = __ballot_sync(0xffffffffu, valid && flag == kFlagIncl);
+      bad[k] = __ballot_sync(0xffffffffu, !valid);
+      if (first_incl == kLookbackWindow && incl) first_incl = 32 * k + __ffs(incl) - 1;
+    }
+    // every position up to and including first_incl must be published
+    bool wait = false;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int hi = first_incl - 32 * k;  // positions 0..hi of this row are needed
+      if (hi < 0) continue;
+      const unsigned need = hi >= 31 ? 0xffffffffu : ((2u << hi) - 1u);
+      if (bad[k] & need) wait = true;
+    }
+    if (wait) {
+      if (++spins > spin_limit) {
         if (lane == 0) atomicOr(&ctl->err, ERR_TIMEOUT);
         break;
       }
-      __nanosleep(sleep_ns);
-      if (sleep_ns < 1024) sleep_ns <<= 1;
+      __nanosleep(spins < 8 ? 20 : 200);
       continue;
     }
-    unsigned long long v = (lane <= first_incl) ? (sv & ((1ull << 38) - 1)) : 0ull;
+    unsigned long long v = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (32 * k + lane <= first_incl) v += sv[k] & vmask;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
     excl += v;
-    if (first_incl < 32) break;
-    j -= 32;
+    if (first_incl < kLookbackWindow) break;
+    j -= kLookbackWindow;
   }
   if (lane == 0) st_relaxed_u64(&state[i], pack_state(epoch, kFlagIncl, excl + total));
   return excl;
 }
 
+// Staging-buffer placement of window records. The index records (vertex layout) and the
+// instance records are shifted so that the bulk-copied part starts on a 16-byte boundary
+// in shared and in global memory (global face g0 + l0 with (g0 + l0) even, resp. a
+// multiple of 4).
+template <int LAYOUT>
+__device__ __forceinline__ int stage_shift(unsigned long long g) {
+  if (LAYOUT == VOX_LAYOUT_INSTANCED) {
+    const int l0 = (int)((4u - (unsigned)(g & 3ull)) & 3u);
+    return (16 - 4 * l0) & 15;
+  }
+  return (g & 1ull) ? 8 : 0;
+}
+
 // Writes face l of the staging window (chunk-local index f_local) for voxel (x, y, z).
 template <int LAYOUT>
-__device__ __forceinline__ void stage_face(unsigned char* stage, int stage_faces, int l, int dir,
-                                           float tx, float ty, float tz, uint32_t f_local,
+__device__ __forceinline__ void stage_face(unsigned char* stage, int stage_faces, int shift, int l,
+                                           int dir, float tx, float ty, float tz, uint32_t f_local,
                                            const TablesDev* tab) {
   if (LAYOUT == VOX_LAYOUT_INSTANCED) {
-    uint32_t* o = reinterpret_cast<uint32_t*>(stage + (size_t)l * 68);
+    uint32_t* o = reinterpret_cast<uint32_t*>(stage + shift + (size_t)l * 68);
     const float z0 = tx * 0.0f, z1 = ty * 0.0f, z2 = tz * 0.0f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
@@ -499,19 +719,18 @@ __device__ __forceinline__ void stage_face(unsigned char* stage, int stage_faces
     o[16] = tab->tex[dir];
   } else {
     float4* v = reinterpret_cast<float4*>(stage + (size_t)l * 96);
-    const float (*C)[3] = tab->corner[dir];
+    // rotated corners of the direction, 12 floats = 3 float4 (v0xyz v1xyz v2xyz v3xyz)
+    const float4* C = reinterpret_cast<const float4*>(tab->corner[dir]);
+    const float4 c0 = C[0], c1 = C[1], c2 = C[2];
     const float face = __uint_as_float(tab->slot[dir]);
-    const float p0x = C[0][0] + tx, p0y = C[0][1] + ty, p0z = C[0][2] + tz;
-    const float p1x = C[1][0] + tx, p1y = C[1][1] + ty, p1z = C[1][2] + tz;
-    const float p2x = C[2][0] + tx, p2y = C[2][1] + ty, p2z = C[2][2] + tz;
-    const float p3x = C[3][0] + tx, p3y = C[3][1] + ty, p3z = C[3][2] + tz;
-    v[0] = make_float4(p0x, p0y, p0z, tab->uv[0][0]);
-    v[1] = make_float4(tab->uv[0][1], face, p1x, p1y);
-    v[2] = make_float4(p1z, tab->uv[1][0], tab->uv[1][1], face);
-    v[3] = make_float4(p2x, p2y, p2z, tab->uv[2][0]);
-    v[4] = make_float4(tab->uv[2][1], face, p3x, p3y);
-    v[5] = make_float4(p3z, tab->uv[3][0], tab->uv[3][1], face);
-    uint2* ix = reinterpret_cast<uint2*>(stage + (size_t)stage_faces * 96 + (size_t)l * 24);
+    // tex coords of quad::VERTICES (src/quad.rs:66-87): (0,0) (1,0) (0,1) (1,1)
+    v[0] = make_float4(c0.x + tx, c0.y + ty, c0.z + tz, 0.0f);
+    v[1] = make_float4(0.0f, face, c0.w + tx, c1.x + ty);
+    v[2] = make_float4(c1.y + tz, 1.0f, 0.0f, face);
+    v[3] = make_float4(c1.z + tx, c1.w + ty, c2.x + tz, 0.0f);
+    v[4] = make_float4(1.0f, face, c2.y + tx, c2.z + ty);
+    v[5] = make_float4(c2.w + tz, 1.0f, 1.0f, face);
+    uint2* ix = reinterpret_cast<uint2*>(stage + (size_t)stage_faces * 96 + shift + (size_t)l * 24);
     const uint32_t b = 4u * f_local;
     ix[0] = make_uint2(b + 0u, b + 2u);
     ix[1] = make_uint2(b + 1u, b + 3u);
@@ -519,88 +738,233 @@ __device__ __forceinline__ void stage_face(unsigned char* stage, int stage_faces
   }
 }
 
-// Copies `nw` staged faces to the global output starting at face index g.
+// Sends `nw` staged faces to the global output starting at face index g: the aligned
+// bulk is one TMA bulk copy issued by thread 0; the few unaligned head/tail records are
+// copied word by word by the other threads. Call after fence + barrier; thread 0 waits
+// until the copies have read the staging buffer before returning.
 template <int LAYOUT>
-__device__ __forceinline__ void flush_stage(const unsigned char* stage, int stage_faces, int nw,
-                                            unsigned long long g, void* out0, void* out1) {
+__device__ __forceinline__ void flush_stage(const unsigned char* stage, int stage_faces, int shift,
+                                            int nw, unsigned long long g, void* out0, void* out1) {
   if (nw <= 0) return;
+  const int t = threadIdx.x;
+  unsigned char* o0 = reinterpret_cast<unsigned char*>(out0);
   if (LAYOUT == VOX_LAYOUT_INSTANCED) {
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(stage);
-    uint32_t* dst = reinterpret_cast<uint32_t*>(out0) + g * 17ull;
-    const int words = nw * 17;
-    for (int q = threadIdx.x; q < words; q += blockDim.x) dst[q] = src[q];
+    int l0 = (int)((4u - (unsigned)(g & 3ull)) & 3u);
+    if (l0 > nw) l0 = nw;
+    const int l1 = l0 + ((nw - l0) & ~3);
+    const unsigned char* src = stage + shift;
+    if (t == 0 && l1 > l0)
+      bulk_s2g_pieces(o0 + (g + l0) * 68ull, src + (size_t)l0 * 68, (uint32_t)(l1 - l0) * 68u);
+    // head faces [0, l0) and tail faces [l1, nw), 17 words each
+    const int head = l0 * 17, tail = (nw - l1) * 17;
+    for (int q = t - 1; q >= 0 && q < head + tail; q += blockDim.x - 1) {
+      const int w = q < head ? q : (l1 * 17 + (q - head));
+      reinterpret_cast<uint32_t*>(o0 + g * 68ull)[w] = reinterpret_cast<const uint32_t*>(src)[w];
+    }
   } else {
-    const float4* src = reinterpret_cast<const float4*>(stage);
-    float4* dst = reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(out0) + g * 96ull);
-    const int v4 = nw * 6;
-    for (int q = threadIdx.x; q < v4; q += blockDim.x) dst[q] = src[q];
-    const uint2* isrc = reinterpret_cast<const uint2*>(stage + (size_t)stage_faces * 96);
-    uint2* idst = reinterpret_cast<uint2*>(reinterpret_cast<unsigned char*>(out1) + g * 24ull);
-    const int i2 = nw * 3;
-    for (int q = threadIdx.x; q < i2; q += blockDim.x) idst[q] = isrc[q];
+    unsigned char* o1 = reinterpret_cast<unsigned char*>(out1);
+    const int l0 = (int)(g & 1ull) < nw ? (int)(g & 1ull) : nw;
+    const int l1 = l0 + ((nw - l0) & ~1);
+    const unsigned char* isrc = stage + (size_t)stage_faces * 96 + shift;
+    if (t == 0) {
+      bulk_s2g_pieces(o0 + g * 96ull, stage, (uint32_t)nw * 96u);
+      if (l1 > l0)
+        bulk_s2g_pieces(o1 + (g + l0) * 24ull, isrc + (size_t)l0 * 24, (uint32_t)(l1 - l0) * 24u);
+    }
+    const int head = l0 * 6, tail = (nw - l1) * 6;
+    for (int q = t - 1; q >= 0 && q < head + tail; q += blockDim.x - 1) {
+      const int w = q < head ? q : (l1 * 6 + (q - head));
+      reinterpret_cast<uint32_t*>(o1 + g * 24ull)[w] = reinterpret_cast<const uint32_t*>(isrc)[w];
+    }
+  }
+  if (t == 0) {
+    bulk_commit();
+    bulk_wait_read_all();
   }
 }
 
+// A face of a warp's face list: local voxel (x, y, z) and emission direction.
+__device__ __forceinline__ uint32_t pack_face(int x, int y, int z, int d) {
+  return (uint32_t)x | ((uint32_t)y << 7) | ((uint32_t)z << 14) | ((uint32_t)d << 21);
+}
+
+// Face compaction of one warp: lane l owns element base + l of the window's rows with
+// faces (rows nz[k0..], N voxels each, so the warp's voxels are consecutive in emission
+// order). Each lane lists its voxel's faces in direction order into the warp's face list;
+// returns the warp's face count and, in `first`, the window-relative index of the warp's
+// first face (face i of the list has index first + i).
+template <int N, int LAYOUT>
+__device__ __forceinline__ int warp_faces(const ChunkSmem<N, LAYOUT>& s, int k0, int elems,
+                                          int base, uint32_t f0, uint32_t* list, uint32_t& first) {
+  using RowT = typename Shape<N>::RowT;
+  const int lane = threadIdx.x & 31;
+  const int e = base + lane;
+  unsigned bits = 0;
+  uint32_t mine = 0;
+  int x = 0, y = 0, z = 0;
+  if (e < elems) {
+    const int r = s.nz[k0 + e / N];
+    x = e % N;
+    y = r / N;
+    z = r % N;
+    RowT m[6];
+    row_masks<N, LAYOUT>(s, y, z, m);
+    const RowT below = x == 0 ? (RowT)0 : ((RowT)(~(RowT)0) >> (sizeof(RowT) * 8 - x));
+    uint32_t pre = 0;
+#pragma unroll
+    for (int d = 0; d < 6; ++d) {
+      pre += (uint32_t)popc_row(m[d] & below);
+      bits |= (unsigned)((m[d] >> x) & (RowT)1) << d;
+    }
+    mine = s.rows[r] - f0 + pre;
+  }
+  const int cnt = __popc(bits);
+  int incl = cnt;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, off);
+    if (lane >= off) incl += v;
+  }
+  const int total = __shfl_sync(0xffffffffu, incl, 31);
+  first = __shfl_sync(0xffffffffu, mine, 0);  // lane 0's voxel starts the warp's range
+  int pos = incl - cnt;
+  while (bits) {
+    const int d = __ffs(bits) - 1;
+    bits &= bits - 1u;
+    list[pos++] = pack_face(x, y, z, d);
+  }
+  __syncwarp();
+  return total;
+}
+
+// Window of rows with faces [k0, k1) holding at most stage_faces faces (at least one row);
+// computed by one thread into misc[1..3] = (k1, first face, faces).
+template <int N, int LAYOUT>
+__device__ __forceinline__ void next_window(ChunkSmem<N, LAYOUT>& s, int k0, int nzc,
+                                            int stage_faces) {
+  const uint32_t f0 = s.rows[s.nz[k0]];
+  int lo = k0 + 1, hi = nzc;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (s.rows[s.nz[mid - 1] + 1] - f0 <= (uint32_t)stage_faces) lo = mid;
+    else hi = mid - 1;
+  }
+  s.misc[1] = lo;
+  s.misc[2] = (int)f0;
+  s.misc[3] = (int)(s.rows[s.nz[lo - 1] + 1] - f0);
+}
+
 // Emits the faces of the chunk in reference order: chunk-local face f goes to global
-// face g0 + f. Windows of whole rows holding at most stage_faces faces are staged in
-// shared memory and flushed with coalesced stores.
+// face g0 + f. Windows of consecutive rows with faces, holding at most stage_faces faces,
+// are staged in shared memory face-parallel (every lane writes one face record) and sent
+// to global memory with TMA bulk copies.
 template <int N, int LAYOUT>
 __device__ void emit_chunk(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c, unsigned long long g0,
                            unsigned long long cap, int stage_faces, void* out0, void* out1) {
-  using RowT = typename Shape<N>::RowT;
-  constexpr int R = Shape<N>::R;
-  const uint32_t total = s.rows[R];
-  if (total == 0) return;
+  const int nzc = s.misc[0];
+  if (nzc == 0) return;
   const int ox = c.x * N, oy = c.y * N, oz = c.z * N;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  int r0 = 0;
-  while (r0 < R) {
-    const uint32_t f0 = s.rows[r0];
-    if (f0 >= total) break;
-    // Largest r1 with rows[r1] - f0 <= stage_faces (binary search; at least one row).
-    int lo = r0 + 1, hi = R;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (s.rows[mid] - f0 <= (uint32_t)stage_faces) lo = mid;
-      else hi = mid - 1;
-    }
-    const int r1 = lo;
-    const int nf = (int)(s.rows[r1] - f0);
-    // Voxel-parallel staging: each lane owns one voxel of a row segment.
-    const int elems = (r1 - r0) * N;
-    for (int base = warp * 32; base < elems; base += nwarps * 32) {
-      const int e = base + lane;
-      const bool live = e < elems;
-      const int r = r0 + (live ? e / N : 0);
-      const int x = live ? e % N : 0;
-      const int y = r / N, z = r % N;
-      const uint32_t rs = s.rows[r];
-      if (live && s.rows[r + 1] != rs) {
-        RowT m[6];
-        row_masks<N, LAYOUT>(s, y, z, m);
-        const RowT below = x == 0 ? (RowT)0 : ((RowT)(~(RowT)0) >> (sizeof(RowT) * 8 - x));
-        uint32_t pre = 0;
-#pragma unroll
-        for (int d = 0; d < 6; ++d) pre += (uint32_t)popc_row(m[d] & below);
-        int l = (int)(rs - f0 + pre);
-        const float tx = (float)(ox + x), ty = (float)(oy + y), tz = (float)(oz + z);
-#pragma unroll
-        for (int d = 0; d < 6; ++d) {
-          if ((m[d] >> x) & (RowT)1) {
-            stage_face<LAYOUT>(s.stage, stage_faces, l, d, tx, ty, tz, f0 + (uint32_t)l, s.tab);
-            ++l;
-          }
-        }
-      }
-    }
-    __syncthreads();
+  uint32_t* list = s.lists + warp * kWarpFaces;
+  if (threadIdx.x == 0) next_window(s, 0, nzc, stage_faces);
+  __syncthreads();
+  int k0 = 0;
+  while (true) {
+    const int k1 = s.misc[1];
+    const uint32_t f0 = (uint32_t)s.misc[2];
+    const int nf = s.misc[3];
     const unsigned long long g = g0 + f0;
+    const int shift = stage_shift<LAYOUT>(g);
+    const int elems = (k1 - k0) * N;
+    for (int base = warp * 32; base < elems; base += nwarps * 32) {
+      uint32_t first;
+      const int nwf = warp_faces<N, LAYOUT>(s, k0, elems, base, f0, list, first);
+      for (int i = lane; i < nwf; i += 32) {
+        const uint32_t q = list[i];
+        const int x = q & 127, y = (q >> 7) & 127, z = (q >> 14) & 127, d = q >> 21;
+        const uint32_t l = first + (uint32_t)i;
+        stage_face<LAYOUT>(s.stage, stage_faces, shift, (int)l, d, (float)(ox + x),
+                           (float)(oy + y), (float)(oz + z), f0 + l, s.tab);
+      }
+      __syncwarp();
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
     int nw = nf;
     if (g >= cap) nw = 0;
     else if (g + (unsigned long long)nf > cap) nw = (int)(cap - g);
-    flush_stage<LAYOUT>(s.stage, stage_faces, nw, g, out0, out1);
+    flush_stage<LAYOUT>(s.stage, stage_faces, shift, nw, g, out0, out1);
+    if (threadIdx.x == 0 && k1 < nzc) next_window(s, k1, nzc, stage_faces);
     __syncthreads();
-    r0 = r1;
+    if (k1 >= nzc) break;
+    k0 = k1;
+  }
+}
+
+// Writes one face record straight to global memory (face index g).
+template <int LAYOUT>
+__device__ __forceinline__ void store_face(void* out0, void* out1, unsigned long long g, int dir,
+                                           float tx, float ty, float tz, uint32_t f_local,
+                                           const TablesDev* tab) {
+  if (LAYOUT == VOX_LAYOUT_INSTANCED) {
+    uint32_t* o = reinterpret_cast<uint32_t*>(out0) + g * 17ull;
+    const float z0 = tx * 0.0f, z1 = ty * 0.0f, z2 = tz * 0.0f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      o[4 * c + 0] = __float_as_uint(tab->part[dir][0][c] + z0);
+      o[4 * c + 1] = __float_as_uint(tab->part[dir][1][c] + z1);
+      o[4 * c + 2] = __float_as_uint(tab->part[dir][2][c] + z2);
+      o[4 * c + 3] = __float_as_uint(tab->row3[dir][c]);
+    }
+    o[12] = __float_as_uint(tx);
+    o[13] = __float_as_uint(ty);
+    o[14] = __float_as_uint(tz);
+    o[15] = __float_as_uint(1.0f);
+    o[16] = tab->tex[dir];
+  } else {
+    float4* v = reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(out0) + g * 96ull);
+    const float4* C = reinterpret_cast<const float4*>(tab->corner[dir]);
+    const float4 c0 = C[0], c1 = C[1], c2 = C[2];
+    const float face = __uint_as_float(tab->slot[dir]);
+    v[0] = make_float4(c0.x + tx, c0.y + ty, c0.z + tz, 0.0f);
+    v[1] = make_float4(0.0f, face, c0.w + tx, c1.x + ty);
+    v[2] = make_float4(c1.y + tz, 1.0f, 0.0f, face);
+    v[3] = make_float4(c1.z + tx, c1.w + ty, c2.x + tz, 0.0f);
+    v[4] = make_float4(1.0f, face, c2.y + tx, c2.z + ty);
+    v[5] = make_float4(c2.w + tz, 1.0f, 1.0f, face);
+    uint2* ix = reinterpret_cast<uint2*>(reinterpret_cast<unsigned char*>(out1) + g * 24ull);
+    const uint32_t b = 4u * f_local;
+    ix[0] = make_uint2(b + 0u, b + 2u);
+    ix[1] = make_uint2(b + 1u, b + 3u);
+    ix[2] = make_uint2(b + 1u, b + 2u);
+  }
+}
+
+// Direct variant of emit_chunk: no staging window and no barrier; after the same
+// face compaction every lane writes one face record straight to global memory, so the
+// 32 lanes of a warp write 32 consecutive faces.
+template <int N, int LAYOUT>
+__device__ void emit_chunk_direct(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c,
+                                  unsigned long long g0, unsigned long long cap, void* out0,
+                                  void* out1) {
+  const int nzc = s.misc[0];
+  const int ox = c.x * N, oy = c.y * N, oz = c.z * N;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  uint32_t* list = s.lists + warp * kWarpFaces;
+  const int elems = nzc * N;
+  for (int base = warp * 32; base < elems; base += nwarps * 32) {
+    uint32_t first;
+    const int nwf = warp_faces<N, LAYOUT>(s, 0, elems, base, 0u, list, first);
+    for (int i = lane; i < nwf; i += 32) {
+      const uint32_t q = list[i];
+      const int x = q & 127, y = (q >> 7) & 127, z = (q >> 14) & 127, d = q >> 21;
+      const uint32_t l = first + (uint32_t)i;
+      const unsigned long long gg = g0 + l;
+      if (gg < cap)
+        store_face<LAYOUT>(out0, out1, gg, d, (float)(ox + x), (float)(oy + y), (float)(oz + z),
+                           l, s.tab);
+    }
+    __syncwarp();
   }
 }
 
@@ -609,13 +973,13 @@ __device__ void emit_chunk(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c, unsigned 
 // ------------------------------------------------------------------------------------
 
 // Persistent fused generation + meshing over a device work queue (GM != GM_OCC), or
-// meshing of resident occupancy (GM == GM_OCC). One chunk per CTA iteration.
-template <int N, int GM, int LAYOUT>
-__global__ void __launch_bounds__(Shape<N>::THREADS)
+// meshing of resident occupancy (GM == GM_OCC). One chunk per CTA iteration; T threads.
+template <int N, int GM, int LAYOUT, int T>
+__global__ void __launch_bounds__(T)
 k_mesh_batch(MeshArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ChunkSmem<N, LAYOUT> s;
-  s.carve(smem_raw, a.stage_faces);
+  s.carve(smem_raw);
   load_tables<N, LAYOUT>(s, a.tables);
   __shared__ int s_item;
   __shared__ unsigned long long s_base;
@@ -663,11 +1027,12 @@ k_mesh_batch(MeshArgs a) {
       unsigned m = a.nbr_mask ? a.nbr_mask[i] : 0u;
       if (GM == GM_BERNOULLI) m = 0u;
       if (!a.full6) m &= 0xFu;
-      gen_chunk<N, GM, LAYOUT>(s, a.gen, c, a.index_base + i, m, true);
+      gen_chunk<N, GM, LAYOUT, T>(s, a.gen, c, a.index_base + i, m, true);
     }
-    const uint32_t total = count_and_scan<N, LAYOUT>(s);
+    const uint32_t total = count_and_scan<N, LAYOUT, T>(s);
     if (threadIdx.x < 32) {
-      const unsigned long long excl = lookback(a.state, a.ctl, epoch, i, total);
+      const unsigned long long excl =
+          lookback(a.state, a.ctl, epoch, i, total, a.spin_limit);
       if (threadIdx.x == 0) {
         s_base = excl;
         a.face_offsets[i] = excl;
@@ -678,42 +1043,46 @@ k_mesh_batch(MeshArgs a) {
       }
     }
     __syncthreads();
-    emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.stage_faces, a.out0, a.out1);
+    if (a.stage_faces > 0) emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.stage_faces, a.out0, a.out1);
+    else emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1);
     __syncthreads();
   }
+  if (threadIdx.x == 0) bulk_wait_all();
 }
 
 // Plain per-chunk mesher: one chunk, one CTA, one launch (no queue, no look-back).
-template <int N, int LAYOUT>
-__global__ void __launch_bounds__(Shape<N>::THREADS)
+template <int N, int LAYOUT, int T>
+__global__ void __launch_bounds__(T)
 k_mesh_single(MeshArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ChunkSmem<N, LAYOUT> s;
-  s.carve(smem_raw, a.stage_faces);
+  s.carve(smem_raw);
   load_tables<N, LAYOUT>(s, a.tables);
   unsigned use = 0;
   for (int d = 0; d < 6; ++d)
     if (a.occ_nbr[d] && (d < 4 || a.full6)) use |= 1u << d;
   load_chunk<N, LAYOUT>(s, a.occ_self, a.occ_nbr, use);
-  const uint32_t total = count_and_scan<N, LAYOUT>(s);
+  const uint32_t total = count_and_scan<N, LAYOUT, T>(s);
   if (threadIdx.x == 0) {
     a.face_offsets[0] = total;
     if ((unsigned long long)total > a.cap) atomicOr(&a.ctl->err, ERR_CAPACITY);
   }
-  emit_chunk<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.stage_faces, a.out0, a.out1);
+  if (a.stage_faces > 0) emit_chunk<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.stage_faces, a.out0, a.out1);
+  else emit_chunk_direct<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.out0, a.out1);
+  if (threadIdx.x == 0) bulk_wait_all();
 }
 
 // Chunk::new for n chunks: one CTA per chunk, occupancy rows written to global memory.
-template <int N, int GM>
-__global__ void __launch_bounds__(Shape<N>::THREADS)
+template <int N, int GM, int T>
+__global__ void __launch_bounds__(T)
 k_generate(MeshArgs a, uint32_t* occ_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ChunkSmem<N, VOX_LAYOUT_VERTEX> s;
-  s.carve(smem_raw, a.stage_faces);
+  s.carve(smem_raw);
   load_tables<N, VOX_LAYOUT_VERTEX>(s, a.tables);
   __syncthreads();
   const int i = blockIdx.x;
-  gen_chunk<N, GM, VOX_LAYOUT_VERTEX>(s, a.gen, a.coords[i], a.index_base + i, 0u, false);
+  gen_chunk<N, GM, VOX_LAYOUT_VERTEX, T>(s, a.gen, a.coords[i], a.index_base + i, 0u, false);
   constexpr int words = N * N * Shape<N>::W;
   const uint32_t* src = reinterpret_cast<const uint32_t*>(s.occ);
   uint32_t* dst = occ_out + (size_t)i * words;

@@ -6,13 +6,14 @@
 namespace vox {
 
 struct KernelSet {
-  int n_size;                // chunk size N
-  int threads;               // CTA size of every kernel of the set
-  const void* batch[4][2];   // k_mesh_batch<N, gen mode, layout>
-  const void* single[2];     // k_mesh_single<N, layout>
-  const void* generate[4];   // k_generate<N, gen mode> (index 0 unused)
-  int smem_fixed[2];         // bytes before the staging window, per layout
-  int (*smem_total)(int layout, int stage_faces);
+  int n_size;                   // chunk size N
+  int threads[2];               // the two CTA sizes the meshing kernels exist in
+  const void* batch[4][2][2];   // k_mesh_batch<N, gen mode, layout, threads[t]>
+  const void* single[2][2];     // k_mesh_single<N, layout, threads[t]>
+  const void* generate[4];      // k_generate<N, gen mode, gen_threads> (index 0 unused)
+  int gen_threads;
+  // dynamic shared memory of a launch (layout, CTA size, staging window in faces)
+  int (*smem_total)(int layout, int threads, int stage_faces);
 };
 
 const KernelSet& kernel_set_8();
@@ -30,5 +31,11 @@ struct Planes {
 };
 cudaError_t launch_frustum(const Planes& planes, const void* coords, int n, int extent,
                            uint8_t* visible, cudaStream_t st);
+
+struct BatchCtl;
+// One look-back for chunk 1 of a batch whose chunk 0 never publishes: the wait must give
+// up after spin_limit polls and latch the timeout bit in ctl (the bounded-wait self-test).
+cudaError_t launch_lookback_probe(unsigned long long* state2, BatchCtl* ctl, int spin_limit,
+                                  cudaStream_t st);
 
 }  // namespace vox

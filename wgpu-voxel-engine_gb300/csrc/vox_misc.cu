@@ -108,3 +108,24 @@ cudaError_t launch_frustum(const Planes& planes, const void* coords, int n, int 
 }
 
 }  // namespace vox
+
+// ---------------------------------------------------------------------------------------
+// Bounded-wait self-test: the look-back of chunk 1 waits on chunk 0, which never
+// publishes (its state word is zero). The wait must end after spin_limit polls with the
+// timeout bit latched, leaving the context usable.
+// ---------------------------------------------------------------------------------------
+#include "vox_device.cuh"
+
+namespace vox {
+namespace {
+__global__ void k_lookback_probe(unsigned long long* state2, BatchCtl* ctl, int spin_limit) {
+  if (threadIdx.x < 32) (void)lookback(state2, ctl, 0xABCDEFu, 1, 0ull, spin_limit);
+}
+}  // namespace
+
+cudaError_t launch_lookback_probe(unsigned long long* state2, BatchCtl* ctl, int spin_limit,
+                                  cudaStream_t st) {
+  k_lookback_probe<<<1, 32, 0, st>>>(state2, ctl, spin_limit);
+  return cudaGetLastError();
+}
+}  // namespace vox

@@ -64,7 +64,8 @@ struct MeshArgs {
   const TablesDev* tables;
   GenDev gen;
   int full6;
-  int stage_faces;                   // faces per staging window
+  int stage_faces;                   // faces per staging window (0: direct global stores)
+  int spin_limit;                    // polls before a look-back wait gives up
 };
 
 }  // namespace vox

@@ -61,6 +61,15 @@ class Sizes(ctypes.Structure):
     ]
 
 
+class Tuning(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_int32), ("stage_faces", ctypes.c_int32),
+                ("ctas_per_sm", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {"threads": self.threads, "stage_faces": self.stage_faces,
+                "ctas_per_sm": self.ctas_per_sm}
+
+
 class VoxError(RuntimeError):
     def __init__(self, status: int, what: str, detail: str = ""):
         self.status = status
@@ -96,6 +105,11 @@ _SIGS = {
                                          ctypes.c_uint64, _P]),
     "vox_frustum_planes": (ctypes.c_int, [_P, _P]),
     "vox_frustum_cull": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P]),
+    "vox_ctx_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(Tuning)]),
+    "vox_ctx_set_tuning": (ctypes.c_int, [_P, ctypes.POINTER(Tuning)]),
+    "vox_autotune": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, ctypes.c_int64, _P, _P,
+                                    ctypes.c_uint64, _P, ctypes.c_int32, ctypes.POINTER(Tuning)]),
+    "vox_selftest_lookback_timeout": (ctypes.c_int, [_P, ctypes.c_int32]),
     "vox_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_P)]),
     "vox_host_free": (ctypes.c_int, [_P]),
 }
@@ -257,6 +271,27 @@ class Context:
         if raise_on_error:
             self._check(st, "vox_gen_mesh_host")
         return st
+
+    def tuning(self) -> Tuning:
+        t = Tuning()
+        self._check(self._lib.vox_ctx_get_tuning(self._h, ctypes.byref(t)), "vox_ctx_get_tuning")
+        return t
+
+    def set_tuning(self, threads: int, stage_faces: int, ctas_per_sm: int = 0):
+        t = Tuning(threads, stage_faces, ctas_per_sm, 0)
+        self._check(self._lib.vox_ctx_set_tuning(self._h, ctypes.byref(t)), "vox_ctx_set_tuning")
+
+    def autotune(self, d_coords, d_nbr_mask, n: int, d_out0, d_out1, cap_faces: int, d_offsets,
+                 chunk_index_base: int = 0, iters: int = 3) -> Tuning:
+        t = Tuning()
+        self._check(self._lib.vox_autotune(self._h, _ptr(d_coords), _ptr(d_nbr_mask), n,
+                                           chunk_index_base, _ptr(d_out0), _ptr(d_out1),
+                                           cap_faces, _ptr(d_offsets), iters, ctypes.byref(t)),
+                    "vox_autotune")
+        return t
+
+    def selftest_lookback_timeout(self, spin_limit: int) -> int:
+        return self._lib.vox_selftest_lookback_timeout(self._h, spin_limit)
 
     def frustum_cull(self, planes, d_coords, n: int, d_visible):
         p = (ctypes.c_float * 24)(*[float(v) for v in planes])
