@@ -195,6 +195,23 @@ int vox_gen_mesh_batch(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint
                        int32_t n, int64_t chunk_index_base, void* d_out0, void* d_out1,
                        uint64_t cap_faces, uint64_t* d_face_offsets);
 
+/* No counterpart in the reference. vox_gen_mesh_batch for callers that cannot allocate
+ * device memory: hosts that own all device memory through their own pool, or code that
+ * must not allocate once it runs. No context is needed and nothing is allocated (no
+ * cudaMalloc, cudaFree or allocating library routine): the caller passes the inputs and
+ * outputs as for vox_gen_mesh_batch, the per-config tables travel as a kernel parameter,
+ * and the kernel's scratch is a static array inside the library (about 129 KiB, held by
+ * every GPU that loads the library until the process exits). At most 16384 chunks per
+ * call; larger n returns VOX_ERR_INVALID. Runs on `stream` (a cudaStream_t, NULL = the
+ * default stream) and waits for it; returns the device-side status (VOX_ERR_CAPACITY,
+ * VOX_ERR_TIMEOUT). The first call on a device looks up the scratch array's address
+ * (cudaGetSymbolAddress) and should come before any stream capture. All calls share the
+ * scratch: calls whose work overlaps on the GPU race. */
+int vox_gen_mesh_batch_noalloc(const vox_config* cfg, void* stream,
+                               const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
+                               int32_t n, int64_t chunk_index_base, void* d_out0, void* d_out1,
+                               uint64_t cap_faces, uint64_t* d_face_offsets);
+
 /* Same as vox_gen_mesh_batch with host buffers: copies the inputs in, runs the fused
  * kernel, and copies exactly the emitted faces and the offsets back. Synchronous. */
 int vox_gen_mesh_host(vox_ctx* ctx, const vox_chunk_coord* h_coords, const uint8_t* h_nbr_mask,

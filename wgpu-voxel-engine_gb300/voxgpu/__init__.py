@@ -103,6 +103,9 @@ _SIGS = {
                                           ctypes.c_uint64, _P]),
     "vox_gen_mesh_host": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, ctypes.c_int64, _P, _P,
                                          ctypes.c_uint64, _P]),
+    "vox_gen_mesh_batch_noalloc": (ctypes.c_int, [ctypes.POINTER(Config), _P, _P, _P,
+                                                  ctypes.c_int32, ctypes.c_int64, _P, _P,
+                                                  ctypes.c_uint64, _P]),
     "vox_frustum_planes": (ctypes.c_int, [_P, _P]),
     "vox_frustum_cull": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P]),
     "vox_ctx_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(Tuning)]),
