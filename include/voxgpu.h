@@ -224,8 +224,9 @@ int vox_gen_mesh_host(vox_ctx* ctx, const vox_chunk_coord* h_coords, const uint8
 typedef struct vox_tuning {
   int32_t threads;     /* CTA size; each chunk size has two (8: 32/64, 16: 128/256,
                           32: 256/512, 64: 512/1024) */
-  int32_t stage_faces; /* faces per shared-memory staging window (>= 6 * chunk_size), or 0 for
-                          direct global stores */
+  int32_t stage_faces; /* 0: every lane stores its face records straight to global memory;
+                          32: each warp stages 32 faces at a time in shared memory and
+                          sends them with a TMA bulk copy */
   int32_t ctas_per_sm; /* resident CTAs per SM of the persistent grid; 0 = as many as fit */
   int32_t reserved;
 } vox_tuning;

@@ -45,32 +45,41 @@ void or_perm_init(uint64_t seed, uint8_t p[512]) {
 
 static float fade_f(float t) { return t * t * t * (t * (t * 6.0f - 15.0f) + 10.0f); }
 static float lerp_f(float t, float a, float b) { return a + t * (b - a); }
-static float grad3_f(int h, float x, float y, float z) {
+
+/* Gradient of hash h as coefficients (gx, gy, gz) in {-1, 0, 1}. Perlin's 2002 gradient
+ * picks u = (h < 8 ? x : y) and v = (h < 4 ? y : h == 12 || h == 14 ? x : z) with the
+ * signs of bits 0 and 1; u and v are always different axes, so the gradient is the dot
+ * product with this coefficient vector. The project's noise spec evaluates it as
+ * ((gx*x + gy*y) + gz*z), which equals u' + v' except for the sign of an exact zero. */
+void or_grad_coef(int h, float g[3]) {
   h &= 15;
-  float u = h < 8 ? x : y;
-  float v = h < 4 ? y : ((h == 12 || h == 14) ? x : z);
-  return ((h & 1) ? -u : u) + ((h & 2) ? -v : v);
+  const float su = (h & 1) ? -1.0f : 1.0f, sv = (h & 2) ? -1.0f : 1.0f;
+  g[0] = g[1] = g[2] = 0.0f;
+  g[h < 8 ? 0 : 1] = su;
+  g[h < 4 ? 1 : ((h == 12 || h == 14) ? 0 : 2)] = sv;
+}
+static float grad3_f(int h, float x, float y, float z) {
+  float g[3];
+  or_grad_coef(h, g);
+  return (g[0] * x + g[1] * y) + g[2] * z;
 }
 static float grad2_f(int h, float x, float y) {
-  h &= 15;
-  float u = h < 8 ? x : y;
-  float v = h < 4 ? y : ((h == 12 || h == 14) ? x : 0.0f);
-  return ((h & 1) ? -u : u) + ((h & 2) ? -v : v);
+  float g[3];
+  or_grad_coef(h, g);
+  return g[0] * x + g[1] * y;
 }
 
 static double fade_d(double t) { return t * t * t * (t * (t * 6.0 - 15.0) + 10.0); }
 static double lerp_d(double t, double a, double b) { return a + t * (b - a); }
 static double grad3_d(int h, double x, double y, double z) {
-  h &= 15;
-  double u = h < 8 ? x : y;
-  double v = h < 4 ? y : ((h == 12 || h == 14) ? x : z);
-  return ((h & 1) ? -u : u) + ((h & 2) ? -v : v);
+  float g[3];
+  or_grad_coef(h, g);
+  return ((double)g[0] * x + (double)g[1] * y) + (double)g[2] * z;
 }
 static double grad2_d(int h, double x, double y) {
-  h &= 15;
-  double u = h < 8 ? x : y;
-  double v = h < 4 ? y : ((h == 12 || h == 14) ? x : 0.0);
-  return ((h & 1) ? -u : u) + ((h & 2) ? -v : v);
+  float g[3];
+  or_grad_coef(h, g);
+  return (double)g[0] * x + (double)g[1] * y;
 }
 
 float or_noise3_f32(const uint8_t* p, float x, float y, float z) {

@@ -33,8 +33,11 @@ uint64_t or_splitmix64_next(uint64_t* state);
 /* Seeded permutation: Fisher-Yates over 0..255 driven by splitmix64(seed), doubled to 512. */
 void or_perm_init(uint64_t seed, uint8_t p[512]);
 
-/* Perlin improved noise (SIGGRAPH 2002), FP32 and FP64. noise2 is the z = 0 slice
- * evaluated bilinearly (the z lerp with w = fade(0) = 0 is dropped). */
+/* Gradient coefficients (gx, gy, gz) of hash h (Perlin 2002's 12 edge directions). */
+void or_grad_coef(int h, float g[3]);
+/* Perlin improved noise (SIGGRAPH 2002), FP32 and FP64, with the gradient evaluated as
+ * ((gx*x + gy*y) + gz*z). noise2 is the z = 0 slice evaluated bilinearly (the z lerp with
+ * w = fade(0) = 0 and the gz*z term are dropped). */
 float or_noise2_f32(const uint8_t* p, float x, float y);
 float or_noise3_f32(const uint8_t* p, float x, float y, float z);
 double or_noise2_f64(const uint8_t* p, double x, double y);

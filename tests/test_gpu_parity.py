@@ -342,7 +342,7 @@ def test_every_launch_shape_is_bit_exact(vox, oracle, wlname, sub, layout):
     offs = to_dev(np.zeros(len(coords) + 1, np.uint64))
     tried = 0
     for threads in threads_options(n):
-        for stage in (0, 6 * n, 512, 2048):
+        for stage in (0, 32):
             for cps in (0, 2):
                 try:
                     ctx.set_tuning(threads, stage, cps)
@@ -357,7 +357,7 @@ def test_every_launch_shape_is_bit_exact(vox, oracle, wlname, sub, layout):
                 if b1:
                     assert np.array_equal(to_np(o1, total * b1), w1), tag
                 tried += 1
-    assert tried >= 8
+    assert tried >= 5
     ctx.close()
 
 
@@ -375,7 +375,7 @@ def test_autotune_picks_a_valid_shape(vox, oracle):
     offs = to_dev(np.zeros(len(coords) + 1, np.uint64))
     t = ctx.autotune(d_coords, d_mask, len(coords), o0, o1, total, offs, iters=2)
     assert t.threads in threads_options(16)
-    assert t.stage_faces == 0 or t.stage_faces >= 96
+    assert t.stage_faces in (0, 32)
     got = ctx.tuning()
     assert (got.threads, got.stage_faces, got.ctas_per_sm) == (t.threads, t.stage_faces, t.ctas_per_sm)
     o0.fill_(0)
@@ -407,7 +407,7 @@ def test_bounded_wait_times_out_and_context_survives(vox, oracle):
     ctx.close()
 
 
-@pytest.mark.parametrize("stage", [0, 512])
+@pytest.mark.parametrize("stage", [0, 32])
 def test_single_chunk_direct_and_staged(vox, oracle, stage):
     rng = np.random.default_rng(11)
     cfg = vox.make_config(chunk_size=32)

@@ -20,6 +20,9 @@
 
 using namespace vox;
 
+// Faces per warp staging buffer (the kernels' kWarpBatch).
+constexpr int kWarpStageFaces = 32;
+
 struct vox_ctx {
   vox_config cfg{};
   int device = 0;
@@ -130,13 +133,11 @@ int gen_mode_of(int kind) {
   }
 }
 
-// Staging window of the default tuning: about 48 KB of shared memory per CTA (at least
-// one full row of faces, 6N).
+// Emission mode of the default tuning (before autotuning): direct global stores.
 int default_stage_faces(const KernelSet& ks, int layout) {
-  const int budget = 48 * 1024;
-  int f = 6 * ks.n_size;
-  while (f + 32 <= 4096 && ks.smem_total(layout, ks.threads[0], f + 32) <= budget) f += 32;
-  return f;
+  (void)ks;
+  (void)layout;
+  return 0;
 }
 
 // Allows `fn` up to `smem` bytes of dynamic shared memory (capped at what the device
@@ -156,8 +157,9 @@ int apply_tuning(vox_ctx* ctx, int topt, int stage_faces, int ctas_per_sm) {
   const KernelSet& ks = *ctx->ks;
   const int layout = ctx->cfg.layout;
   if (topt < 0 || topt > 1) return fail(ctx, VOX_ERR_INVALID, "unsupported CTA size");
-  if (stage_faces != 0 && stage_faces < 6 * ks.n_size)
-    return fail(ctx, VOX_ERR_INVALID, "stage_faces must be 0 or at least 6 * chunk_size");
+  if (stage_faces != 0 && stage_faces != kWarpStageFaces)
+    return fail(ctx, VOX_ERR_INVALID, "stage_faces must be 0 (direct stores) or %d",
+                kWarpStageFaces);
   if (ctas_per_sm < 0) return fail(ctx, VOX_ERR_INVALID, "ctas_per_sm must be >= 0");
   const int smem = ks.smem_total(layout, ks.threads[topt], stage_faces);
   if (smem > ctx->max_smem_optin - 256)
@@ -648,7 +650,8 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
   int st = check_outputs(ctx, d_out0, d_out1, cap_faces);
   if (st != VOX_OK) return st;
   const int N = ctx->cfg.chunk_size;
-  const int stages[] = {0, 6 * N, 256, 512, 1024, 2048, 4096};
+  (void)N;
+  const int stages[] = {0, kWarpStageFaces};
   const int ctas[] = {0, 4, 2};
   cudaEvent_t e0, e1;
   VOX_CUDA(ctx, cudaEventCreate(&e0), "cudaEventCreate");
@@ -670,7 +673,6 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
   };
   for (int t = 0; t < 2 && st == VOX_OK; ++t)
     for (int s : stages) {
-      if (s != 0 && s < 6 * N) continue;
       int full_grid = 0;
       for (int c : ctas) {
         if (apply_tuning(ctx, t, s, c) != VOX_OK) continue;

@@ -55,6 +55,15 @@ struct AxisZ {
 constexpr int kOctGroup = 8;
 // Faces one warp's 32 voxels can have (6 each): the size of a warp's face list.
 constexpr int kWarpFaces = 32 * 6;
+// Faces one warp stages at a time (each warp has two staging buffers of this many faces).
+constexpr int kWarpBatch = 32;
+// Bytes of one warp staging buffer (vertex records, then the index records shifted by up
+// to 8 bytes; or instance records shifted by up to 12 bytes).
+template <int LAYOUT>
+__host__ __device__ constexpr int warp_buf_bytes() {
+  return LAYOUT == VOX_LAYOUT_INSTANCED ? align16(kWarpBatch * 68 + 16)
+                                        : kWarpBatch * 96 + align16(kWarpBatch * 24 + 16);
+}
 
 // Shared-memory carve-up; the same functions size the launch on the host.
 template <int N, int LAYOUT>
@@ -76,13 +85,14 @@ struct SmemPlan {
   static constexpr int kAxis = 2 * kAxisHalf;
   static constexpr int kZRange = align16(2 * N * 4);
   static constexpr int kGenScratch = kColK + kAxis + kZRange;
-  __host__ __device__ static int stage_bytes(int faces) {
-    int b = LAYOUT == VOX_LAYOUT_INSTANCED ? align16(faces * 68 + 16)
-                                           : faces * 96 + align16(faces * 24 + 16);
+  // staging area: two buffers per warp when staging (stage_faces > 0), else only the
+  // generation scratch
+  __host__ __device__ static int stage_bytes(int threads, int stage_faces) {
+    const int b = stage_faces > 0 ? (threads / 32) * 2 * warp_buf_bytes<LAYOUT>() : 0;
     return b < kGenScratch ? kGenScratch : b;
   }
-  __host__ __device__ static int total(int threads, int faces) {
-    return fixed(threads) + stage_bytes(faces);
+  __host__ __device__ static int total(int threads, int stage_faces) {
+    return fixed(threads) + stage_bytes(threads, stage_faces);
   }
 };
 
@@ -94,20 +104,18 @@ __device__ __forceinline__ float d_fade(float t) {
   return t * t * t * (t * (t * 6.0f - 15.0f) + 10.0f);
 }
 __device__ __forceinline__ float d_lerp(float t, float a, float b) { return a + t * (b - a); }
-__device__ __forceinline__ float d_grad3(int h, float x, float y, float z) {
-  h &= 15;
-  float u = h < 8 ? x : y;
-  float v = h < 4 ? y : ((h == 12 || h == 14) ? x : z);
-  return ((h & 1) ? -u : u) + ((h & 2) ? -v : v);
+// Gradient dot products from the coefficient table (gx, gy, gz) of hash & 15.
+__device__ __forceinline__ float d_grad3(const float4* gt, int h, float x, float y, float z) {
+  const float4 g = gt[h & 15];
+  return (g.x * x + g.y * y) + g.z * z;
 }
-__device__ __forceinline__ float d_grad2(int h, float x, float y) {
-  h &= 15;
-  float u = h < 8 ? x : y;
-  float v = h < 4 ? y : ((h == 12 || h == 14) ? x : 0.0f);
-  return ((h & 1) ? -u : u) + ((h & 2) ? -v : v);
+__device__ __forceinline__ float d_grad2(const float4* gt, int h, float x, float y) {
+  const float4 g = gt[h & 15];
+  return g.x * x + g.y * y;
 }
 
-__device__ __forceinline__ float d_noise3(const uint8_t* p, float x, float y, float z) {
+__device__ __forceinline__ float d_noise3(const uint8_t* p, const float4* gt, float x, float y,
+                                          float z) {
   float fx = floorf(x), fy = floorf(y), fz = floorf(z);
   int X = (int)fx & 255, Y = (int)fy & 255, Z = (int)fz & 255;
   x = x - fx;
@@ -117,29 +125,31 @@ __device__ __forceinline__ float d_noise3(const uint8_t* p, float x, float y, fl
   int A = p[X] + Y, AA = p[A] + Z, AB = p[A + 1] + Z;
   int B = p[X + 1] + Y, BA = p[B] + Z, BB = p[B + 1] + Z;
   float x1 = x - 1.0f, y1 = y - 1.0f, z1 = z - 1.0f;
-  float l00 = d_lerp(u, d_grad3(p[AA], x, y, z), d_grad3(p[BA], x1, y, z));
-  float l10 = d_lerp(u, d_grad3(p[AB], x, y1, z), d_grad3(p[BB], x1, y1, z));
-  float l01 = d_lerp(u, d_grad3(p[AA + 1], x, y, z1), d_grad3(p[BA + 1], x1, y, z1));
-  float l11 = d_lerp(u, d_grad3(p[AB + 1], x, y1, z1), d_grad3(p[BB + 1], x1, y1, z1));
+  float l00 = d_lerp(u, d_grad3(gt, p[AA], x, y, z), d_grad3(gt, p[BA], x1, y, z));
+  float l10 = d_lerp(u, d_grad3(gt, p[AB], x, y1, z), d_grad3(gt, p[BB], x1, y1, z));
+  float l01 = d_lerp(u, d_grad3(gt, p[AA + 1], x, y, z1), d_grad3(gt, p[BA + 1], x1, y, z1));
+  float l11 = d_lerp(u, d_grad3(gt, p[AB + 1], x, y1, z1), d_grad3(gt, p[BB + 1], x1, y1, z1));
   return d_lerp(w, d_lerp(v, l00, l10), d_lerp(v, l01, l11));
 }
 
 // noise2 at a column whose per-axis lattice data were computed once per octave; the
 // operations are those of the oracle's or_noise2_f32, minus the shared subexpressions.
-__device__ __forceinline__ float d_noise2_axes(const uint8_t* p, const AxisX& ax, const AxisZ& az) {
+__device__ __forceinline__ float d_noise2_axes(const uint8_t* p, const float4* gt, const AxisX& ax,
+                                               const AxisZ& az) {
   const int A = ax.px + az.y, B = ax.px1 + az.y;
   const float x = ax.fr, y = az.fr;
   const float x1 = x - 1.0f, y1 = y - 1.0f;
-  const float l0 = d_lerp(ax.u, d_grad2(p[p[A]], x, y), d_grad2(p[p[B]], x1, y));
-  const float l1 = d_lerp(ax.u, d_grad2(p[p[A + 1]], x, y1), d_grad2(p[p[B + 1]], x1, y1));
+  const float l0 = d_lerp(ax.u, d_grad2(gt, p[p[A]], x, y), d_grad2(gt, p[p[B]], x1, y));
+  const float l1 =
+      d_lerp(ax.u, d_grad2(gt, p[p[A + 1]], x, y1), d_grad2(gt, p[p[B + 1]], x1, y1));
   return d_lerp(az.v, l0, l1);
 }
 
-__device__ __forceinline__ float d_fbm3(const uint8_t* p, float x, float y, float z,
-                                        const GenDev& g) {
+__device__ __forceinline__ float d_fbm3(const uint8_t* p, const float4* gt, float x, float y,
+                                        float z, const GenDev& g) {
   float sum = 0.0f, amp = 1.0f, f = g.freq;
   for (int o = 0; o < g.octaves; ++o) {
-    sum = sum + amp * d_noise3(p, x * f, y * f, z * f);
+    sum = sum + amp * d_noise3(p, gt, x * f, y * f, z * f);
     f = f * g.lac;
     amp = amp * g.gain;
   }
@@ -321,6 +331,7 @@ __device__ void gen_heightmap(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, 
   constexpr int CPT = (side * side + T - 1) / T;
   const int t = threadIdx.x;
   const uint8_t* p = s.tab->perm;
+  const float4* gt = reinterpret_cast<const float4*>(s.tab->grad);
   float acc[CPT];
 #pragma unroll
   for (int c = 0; c < CPT; ++c) acc[c] = 0.0f;
@@ -363,7 +374,7 @@ __device__ void gen_heightmap(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, 
         if (!corner) {
           float a = amp, sum = acc[c];
           for (int o = 0; o < no; ++o) {
-            sum = sum + a * d_noise2_axes(p, s.ax[o * side + xi], s.az[o * side + zi]);
+            sum = sum + a * d_noise2_axes(p, gt, s.ax[o * side + xi], s.az[o * side + zi]);
             a = a * g.gain;
           }
           acc[c] = sum;
@@ -433,7 +444,8 @@ __device__ __forceinline__ bool gen_solid(const ChunkSmem<N, LAYOUT>& s, const G
                                           unsigned long long s0) {
   if (GM == GM_DENSITY) {
     const int wy = oy + y;
-    const float f = d_fbm3(s.tab->perm, (float)(ox + x), (float)wy, (float)(oz + z), g);
+    const float f = d_fbm3(s.tab->perm, reinterpret_cast<const float4*>(s.tab->grad),
+                           (float)(ox + x), (float)wy, (float)(oz + z), g);
     const float d = f - ((float)wy - g.y_ref) * g.y_scale;
     return g.solid_below_zero ? (d < 0.0f) : (d > 0.0f);
   } else {  // GM_BERNOULLI
@@ -738,26 +750,28 @@ __device__ __forceinline__ void stage_face(unsigned char* stage, int stage_faces
   }
 }
 
-// Sends `nw` staged faces to the global output starting at face index g: the aligned
-// bulk is one TMA bulk copy issued by thread 0; the few unaligned head/tail records are
-// copied word by word by the other threads. Call after fence + barrier; thread 0 waits
-// until the copies have read the staging buffer before returning.
+// Sends `nw` faces staged in one warp buffer to the global output starting at face
+// index g: lane 0 issues the TMA bulk copies of the 16-byte aligned part and commits them
+// as one bulk group; the few unaligned head/tail records are stored word by word by the
+// other lanes. Call after fence.proxy.async + __syncwarp.
 template <int LAYOUT>
-__device__ __forceinline__ void flush_stage(const unsigned char* stage, int stage_faces, int shift,
-                                            int nw, unsigned long long g, void* out0, void* out1) {
-  if (nw <= 0) return;
-  const int t = threadIdx.x;
+__device__ __forceinline__ void flush_warp(const unsigned char* buf, int shift, int nw,
+                                           unsigned long long g, void* out0, void* out1) {
+  const int lane = threadIdx.x & 31;
   unsigned char* o0 = reinterpret_cast<unsigned char*>(out0);
   if (LAYOUT == VOX_LAYOUT_INSTANCED) {
     int l0 = (int)((4u - (unsigned)(g & 3ull)) & 3u);
     if (l0 > nw) l0 = nw;
     const int l1 = l0 + ((nw - l0) & ~3);
-    const unsigned char* src = stage + shift;
-    if (t == 0 && l1 > l0)
-      bulk_s2g_pieces(o0 + (g + l0) * 68ull, src + (size_t)l0 * 68, (uint32_t)(l1 - l0) * 68u);
+    const unsigned char* src = buf + shift;
+    if (lane == 0) {
+      if (l1 > l0)
+        bulk_s2g(o0 + (g + l0) * 68ull, src + (size_t)l0 * 68, (uint32_t)(l1 - l0) * 68u);
+      bulk_commit();
+    }
     // head faces [0, l0) and tail faces [l1, nw), 17 words each
     const int head = l0 * 17, tail = (nw - l1) * 17;
-    for (int q = t - 1; q >= 0 && q < head + tail; q += blockDim.x - 1) {
+    for (int q = lane - 1; q >= 0 && q < head + tail; q += 31) {
       const int w = q < head ? q : (l1 * 17 + (q - head));
       reinterpret_cast<uint32_t*>(o0 + g * 68ull)[w] = reinterpret_cast<const uint32_t*>(src)[w];
     }
@@ -765,21 +779,18 @@ __device__ __forceinline__ void flush_stage(const unsigned char* stage, int stag
     unsigned char* o1 = reinterpret_cast<unsigned char*>(out1);
     const int l0 = (int)(g & 1ull) < nw ? (int)(g & 1ull) : nw;
     const int l1 = l0 + ((nw - l0) & ~1);
-    const unsigned char* isrc = stage + (size_t)stage_faces * 96 + shift;
-    if (t == 0) {
-      bulk_s2g_pieces(o0 + g * 96ull, stage, (uint32_t)nw * 96u);
+    const unsigned char* isrc = buf + kWarpBatch * 96 + shift;
+    if (lane == 0) {
+      bulk_s2g(o0 + g * 96ull, buf, (uint32_t)nw * 96u);
       if (l1 > l0)
-        bulk_s2g_pieces(o1 + (g + l0) * 24ull, isrc + (size_t)l0 * 24, (uint32_t)(l1 - l0) * 24u);
+        bulk_s2g(o1 + (g + l0) * 24ull, isrc + (size_t)l0 * 24, (uint32_t)(l1 - l0) * 24u);
+      bulk_commit();
     }
     const int head = l0 * 6, tail = (nw - l1) * 6;
-    for (int q = t - 1; q >= 0 && q < head + tail; q += blockDim.x - 1) {
+    for (int q = lane - 1; q >= 0 && q < head + tail; q += 31) {
       const int w = q < head ? q : (l1 * 6 + (q - head));
       reinterpret_cast<uint32_t*>(o1 + g * 24ull)[w] = reinterpret_cast<const uint32_t*>(isrc)[w];
     }
-  }
-  if (t == 0) {
-    bulk_commit();
-    bulk_wait_read_all();
   }
 }
 
@@ -809,12 +820,15 @@ __device__ __forceinline__ int warp_faces(const ChunkSmem<N, LAYOUT>& s, int k0,
     z = r % N;
     RowT m[6];
     row_masks<N, LAYOUT>(s, y, z, m);
-    const RowT below = x == 0 ? (RowT)0 : ((RowT)(~(RowT)0) >> (sizeof(RowT) * 8 - x));
-    uint32_t pre = 0;
 #pragma unroll
-    for (int d = 0; d < 6; ++d) {
-      pre += (uint32_t)popc_row(m[d] & below);
-      bits |= (unsigned)((m[d] >> x) & (RowT)1) << d;
+    for (int d = 0; d < 6; ++d) bits |= (unsigned)((m[d] >> x) & (RowT)1) << d;
+    // Only lane 0's position is needed (the warp scan places the others). A warp starts
+    // on a row boundary (x = 0) unless rows are 64 wide (x = 0 or 32).
+    uint32_t pre = 0;
+    if (N > 32 && lane == 0 && x != 0) {
+      const RowT below = (RowT)(~(RowT)0) >> (sizeof(RowT) * 8 - x);
+#pragma unroll
+      for (int d = 0; d < 6; ++d) pre += (uint32_t)popc_row(m[d] & below);
     }
     mine = s.rows[r] - f0 + pre;
   }
@@ -837,68 +851,54 @@ __device__ __forceinline__ int warp_faces(const ChunkSmem<N, LAYOUT>& s, int k0,
   return total;
 }
 
-// Window of rows with faces [k0, k1) holding at most stage_faces faces (at least one row);
-// computed by one thread into misc[1..3] = (k1, first face, faces).
-template <int N, int LAYOUT>
-__device__ __forceinline__ void next_window(ChunkSmem<N, LAYOUT>& s, int k0, int nzc,
-                                            int stage_faces) {
-  const uint32_t f0 = s.rows[s.nz[k0]];
-  int lo = k0 + 1, hi = nzc;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (s.rows[s.nz[mid - 1] + 1] - f0 <= (uint32_t)stage_faces) lo = mid;
-    else hi = mid - 1;
-  }
-  s.misc[1] = lo;
-  s.misc[2] = (int)f0;
-  s.misc[3] = (int)(s.rows[s.nz[lo - 1] + 1] - f0);
-}
-
 // Emits the faces of the chunk in reference order: chunk-local face f goes to global
-// face g0 + f. Windows of consecutive rows with faces, holding at most stage_faces faces,
-// are staged in shared memory face-parallel (every lane writes one face record) and sent
-// to global memory with TMA bulk copies.
+// face g0 + f. Every warp compacts the faces of its 32 voxels, stages them 32 at a time
+// in one of its two shared-memory buffers (one face record per lane, final byte layout)
+// and sends each batch to global memory with a TMA bulk copy issued by its lane 0. No
+// CTA-wide barrier: a warp waits only until the bulk copy that last read a buffer is
+// done before refilling it, and until all its copies have read shared memory at the end
+// (the staging area is reused by the next chunk's generation).
 template <int N, int LAYOUT>
 __device__ void emit_chunk(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c, unsigned long long g0,
-                           unsigned long long cap, int stage_faces, void* out0, void* out1) {
+                           unsigned long long cap, void* out0, void* out1) {
+  constexpr int kBuf = warp_buf_bytes<LAYOUT>();
   const int nzc = s.misc[0];
-  if (nzc == 0) return;
   const int ox = c.x * N, oy = c.y * N, oz = c.z * N;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   uint32_t* list = s.lists + warp * kWarpFaces;
-  if (threadIdx.x == 0) next_window(s, 0, nzc, stage_faces);
-  __syncthreads();
-  int k0 = 0;
-  while (true) {
-    const int k1 = s.misc[1];
-    const uint32_t f0 = (uint32_t)s.misc[2];
-    const int nf = s.misc[3];
-    const unsigned long long g = g0 + f0;
-    const int shift = stage_shift<LAYOUT>(g);
-    const int elems = (k1 - k0) * N;
-    for (int base = warp * 32; base < elems; base += nwarps * 32) {
-      uint32_t first;
-      const int nwf = warp_faces<N, LAYOUT>(s, k0, elems, base, f0, list, first);
-      for (int i = lane; i < nwf; i += 32) {
-        const uint32_t q = list[i];
-        const int x = q & 127, y = (q >> 7) & 127, z = (q >> 14) & 127, d = q >> 21;
-        const uint32_t l = first + (uint32_t)i;
-        stage_face<LAYOUT>(s.stage, stage_faces, shift, (int)l, d, (float)(ox + x),
-                           (float)(oy + y), (float)(oz + z), f0 + l, s.tab);
-      }
+  unsigned char* bufs = s.stage + (size_t)warp * 2 * kBuf;
+  int b = 0;
+  const int elems = nzc * N;
+  for (int base = warp * 32; base < elems; base += nwarps * 32) {
+    uint32_t first;
+    const int nwf = warp_faces<N, LAYOUT>(s, 0, elems, base, 0u, list, first);
+    for (int r0 = 0; r0 < nwf; r0 += kWarpBatch) {
+      const int cnt = nwf - r0 < kWarpBatch ? nwf - r0 : kWarpBatch;
+      const unsigned long long g = g0 + first + (unsigned)r0;
+      int nw = cnt;
+      if (g >= cap) nw = 0;
+      else if (g + (unsigned long long)cnt > cap) nw = (int)(cap - g);
+      if (nw == 0) continue;
+      unsigned char* buf = bufs + b * kBuf;
+      // the copy issued two batches ago read this buffer; wait until it is done reading
+      if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
       __syncwarp();
+      const int shift = stage_shift<LAYOUT>(g);
+      if (lane < nw) {
+        const uint32_t q = list[r0 + lane];
+        const int x = q & 127, y = (q >> 7) & 127, z = (q >> 14) & 127, d = q >> 21;
+        stage_face<LAYOUT>(buf, kWarpBatch, shift, lane, d, (float)(ox + x), (float)(oy + y),
+                           (float)(oz + z), first + (uint32_t)(r0 + lane), s.tab);
+      }
+      fence_proxy_async_smem();
+      __syncwarp();
+      flush_warp<LAYOUT>(buf, shift, nw, g, out0, out1);
+      __syncwarp();
+      b ^= 1;
     }
-    fence_proxy_async_smem();
-    __syncthreads();
-    int nw = nf;
-    if (g >= cap) nw = 0;
-    else if (g + (unsigned long long)nf > cap) nw = (int)(cap - g);
-    flush_stage<LAYOUT>(s.stage, stage_faces, shift, nw, g, out0, out1);
-    if (threadIdx.x == 0 && k1 < nzc) next_window(s, k1, nzc, stage_faces);
-    __syncthreads();
-    if (k1 >= nzc) break;
-    k0 = k1;
   }
+  if (lane == 0) bulk_wait_read_all();
+  __syncwarp();
 }
 
 // Writes one face record straight to global memory (face index g).
@@ -1043,11 +1043,11 @@ k_mesh_batch(MeshArgs a) {
       }
     }
     __syncthreads();
-    if (a.stage_faces > 0) emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.stage_faces, a.out0, a.out1);
+    if (a.stage_faces > 0) emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1);
     else emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1);
     __syncthreads();
   }
-  if (threadIdx.x == 0) bulk_wait_all();
+  if ((threadIdx.x & 31) == 0) bulk_wait_all();  // every lane 0 issued bulk copies
 }
 
 // Plain per-chunk mesher: one chunk, one CTA, one launch (no queue, no look-back).
@@ -1067,9 +1067,9 @@ k_mesh_single(MeshArgs a) {
     a.face_offsets[0] = total;
     if ((unsigned long long)total > a.cap) atomicOr(&a.ctl->err, ERR_CAPACITY);
   }
-  if (a.stage_faces > 0) emit_chunk<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.stage_faces, a.out0, a.out1);
+  if (a.stage_faces > 0) emit_chunk<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.out0, a.out1);
   else emit_chunk_direct<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.out0, a.out1);
-  if (threadIdx.x == 0) bulk_wait_all();
+  if ((threadIdx.x & 31) == 0) bulk_wait_all();
 }
 
 // Chunk::new for n chunks: one CTA per chunk, occupancy rows written to global memory.

@@ -117,6 +117,14 @@ void build_tables(const vox_config& cfg, TablesDev& t) {
     perm[j] = tmp;
   }
   for (int i = 0; i < 512; ++i) t.perm[i] = perm[i & 255];
+  // Gradient of hash h (Perlin 2002): u = x if h < 8 else y, v = y if h < 4, x if h is
+  // 12 or 14, z otherwise; bit 0 negates u, bit 1 negates v. u and v are different axes.
+  for (int h = 0; h < 16; ++h) {
+    float g[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    g[h < 8 ? 0 : 1] = (h & 1) ? -1.0f : 1.0f;
+    g[h < 4 ? 1 : ((h == 12 || h == 14) ? 0 : 2)] = (h & 2) ? -1.0f : 1.0f;
+    for (int k = 0; k < 4; ++k) t.grad[h][k] = g[k];
+  }
 }
 
 }  // namespace vox

@@ -34,6 +34,7 @@ struct TablesDev {
   uint32_t tex[6];        // texture index per emission direction
   uint32_t slot[6];       // face slot per emission direction
   uint8_t perm[512];      // noise permutation
+  float grad[16][4];      // gradient coefficients (gx, gy, gz, 0) of hash & 15
 };
 
 struct BatchCtl {
