@@ -49,7 +49,7 @@ def parse_args():
     p.add_argument("--steps", type=int, default=400)
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--workload", choices=list(WORKLOAD_TEXT), default="heightmap")
+    p.add_argument("--workload", choices=list(WORKLOAD_TEXT) + ["serving"], default="heightmap")
     p.add_argument("--layout", choices=["vertex", "instanced"], default="vertex")
     p.add_argument("--slab", type=int, default=512, help="chunks per launch (stress workload)")
     p.add_argument("--cpu-seconds", type=float, default=8.0,
@@ -60,6 +60,10 @@ def parse_args():
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--tuning", default=None,
                    help="force a launch shape 'threads,stage_faces,ctas_per_sm' (no autotune)")
+    p.add_argument("--frames", type=int, default=10000, help="serving workload: frames")
+    p.add_argument("--paced", action="store_true", help="serving workload: real-time 60 fps")
+    p.add_argument("--latency-frames", type=int, default=300,
+                   help="paced serving frames measured for the headline latency (0: skip)")
     p.add_argument("--tune-iters", type=int, default=5)
     return p.parse_args()
 
@@ -360,6 +364,10 @@ def run_ours(args):
         line["batched_vs_plain"] = value / world / plain["value"]
     if e2e:
         line["e2e"] = e2e
+    if rank == 0 and world == 1 and args.latency_frames > 0 and args.workload == "heightmap":
+        # p50/p99 request-to-mesh latency of the streaming engine at the serving request
+        # rate (real-time 60 frames/s camera), next to the batch throughput above
+        line["latency"] = serving_run(args.latency_frames, paced=True)
     if rank == 0 and world == 1 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline(wl, cfg, masks, args.cpu_seconds)
     if rank == 0:
@@ -456,10 +464,65 @@ def e2e_host(ctx, wl, masks, n, total_faces, b0, b1, args, np):
             "api": "vox_gen_mesh_host (pinned host buffers, synchronous)"}
 
 
+def serving_run(frames: int, paced: bool, view_radius: int = 24, slots: int = 3,
+                max_batch: int = 64):
+    """The serving workload: the simulated camera (20 units/s along +x, 90 deg/s yaw
+    sweep, 60 frames/s) drives the streaming engine over the heightmap terrain (16^3
+    chunks, view radius 24 chunks, 24 GB device cache with LRU eviction). Paced: frame k
+    starts at k/60 s of wall time; unpaced: frames back to back (maximum request rate)."""
+    import voxgpu
+    wl = voxgpu.workload("heightmap")
+    srv = voxgpu.Server(wl.config(), view_radius=view_radius, max_batch=max_batch, slots=slots,
+                        cache_budget_bytes=24 << 30)
+    zfar = (view_radius + 2) * 16.0
+    t0 = voxgpu.Server.now()
+    for k in range(frames):
+        ts = k / 60.0
+        if paced:
+            while voxgpu.Server.now() - t0 < ts:
+                time.sleep(0.0005)
+        eye, d = voxgpu.serving_camera(ts)
+        srv.frame(voxgpu.camera_matrix(eye, d, zfar=zfar), eye)
+    srv.drain()
+    wall = voxgpu.Server.now() - t0
+    st = srv.stats()
+    srv.close()
+    return {
+        "frames": frames, "paced_60fps": paced, "requested": st.requested,
+        "completed": st.completed, "launches": st.launches, "evicted": st.evicted,
+        "p50_ms": st.latency_p50_ms, "p99_ms": st.latency_p99_ms, "max_ms": st.latency_max_ms,
+        "chunks_per_s_busy": st.completed / st.busy_s if st.busy_s > 0 else None,
+        "wall_s": wall, "frame_budget_ms": 1000.0 / 60,
+    }
+
+
+def run_serving(args):
+    rank, world, local = dist_info()
+    import torch
+    torch.cuda.set_device(local)
+    frames = args.frames
+    res = serving_run(frames, args.paced)
+    line = {
+        "metric": METRIC, "value": res["chunks_per_s_busy"], "unit": "chunks/s",
+        "n_gpus": 1, "steps": frames, "warmup": 0, "ms_per_step": res["wall_s"] * 1e3 / frames,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32",
+        "data": "synthetic",
+        "config": {"workload": "serving: simulated camera 20 u/s + 90 deg/s yaw, 60 frames/s, "
+                               "heightmap-fbm 16^3 chunks, view radius 24, 24 GB LRU cache",
+                   "paced": args.paced},
+        "latency": res,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "serving":
+        return run_serving(args)
     return run_ours(args)
 
 

@@ -1,0 +1,94 @@
+/*
+ * voxgpu_serve.h — C ABI of the chunk streaming engine (the request loop that replaces
+ * the reference's ChunkGenerator / World, src/chunk_builder.rs:11-353, src/world.rs:14-59)
+ * and of the camera / coordinate helpers it uses (src/camera.rs:41-51,
+ * src/coordinate.rs:13-65).
+ *
+ * Every frame the engine frustum-culls the chunks within the view radius on the device,
+ * turns the visible chunks that are neither resident nor pending into requests ordered by
+ * distance to the eye, admits them into batches as batch slots free up (several batches
+ * in flight on their own streams: continuous batching), and integrates finished batches
+ * into a device mesh cache kept under a byte budget with least-recently-used eviction.
+ * It records, per chunk, the time from its request to the moment its mesh is resident.
+ *
+ * Unlike the reference (one chunk dispatched and one integrated per 7 frames, meshes
+ * rebuilt as neighbours arrive), a chunk's halo comes from the generator itself, so its
+ * mesh is the final one (all four lateral neighbours present) whatever else is loaded:
+ * the same bytes alone, in any batch, and in any order of arrival.
+ */
+#ifndef VOXGPU_SERVE_H
+#define VOXGPU_SERVE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "voxgpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct vox_serve_config {
+  vox_config chunk;            /* generator, chunk size, culling, layout */
+  int32_t view_radius;         /* chunks: requests only within this xz distance of the eye */
+  int32_t y_min, y_max;        /* chunk layers that are requested (the reference: 0..0) */
+  int32_t max_batch;           /* chunks per launch */
+  int32_t slots;               /* batches in flight at once (one stream each) */
+  uint64_t cache_budget_bytes; /* device bytes for resident meshes (LRU eviction beyond) */
+} vox_serve_config;
+
+typedef struct vox_serve_stats {
+  uint64_t frames;             /* vox_serve_frame calls */
+  uint64_t requested;          /* chunks requested */
+  uint64_t completed;          /* chunks whose mesh became resident */
+  uint64_t evicted;            /* chunks evicted from the cache */
+  uint64_t launches;           /* fused gen+mesh launches */
+  uint64_t faces_resident;     /* faces held by resident chunks */
+  uint64_t cache_bytes;        /* bytes held by resident mesh blocks */
+  uint64_t resident;           /* resident chunks */
+  uint64_t pending;            /* requested, not yet resident */
+  double latency_p50_ms;       /* request -> resident, over all completed chunks */
+  double latency_p99_ms;
+  double latency_max_ms;
+  double busy_s;               /* wall time between the first request and the last completion */
+} vox_serve_stats;
+
+typedef struct vox_serve vox_serve;
+
+int vox_serve_create(const vox_serve_config* cfg, vox_serve** out);
+int vox_serve_destroy(vox_serve* s);
+
+/* The engine's monotonic clock in seconds (request and completion times use it). */
+double vox_serve_now(void);
+
+/* One frame: `view_proj` is the camera's column-major global matrix (frustum planes are
+ * taken from it as in Frustum::matrix_to_planes), `eye` the camera position in world
+ * units, `now_s` the frame's time on the engine clock (negative: read the clock). Culls,
+ * requests, admits new batches and integrates finished ones (a chunk's latency ends when
+ * the engine sees its batch finished); does not wait for the GPU. */
+int vox_serve_frame(vox_serve* s, const float view_proj[16], const float eye[3], double now_s);
+
+/* Waits for every batch in flight (and every queued request) and integrates them. */
+int vox_serve_drain(vox_serve* s);
+
+int vox_serve_get_stats(vox_serve* s, vox_serve_stats* out);
+
+/* The resident mesh of chunk `c`: device pointers to its records (out1 NULL for the
+ * instanced layout) and its face count. Returns VOX_ERR_INVALID if it is not resident. */
+int vox_serve_lookup(vox_serve* s, vox_chunk_coord c, const void** d_out0, const void** d_out1,
+                     uint64_t* faces);
+
+/* Camera::update_global_matrix (src/camera.rs:41-51): OPENGL_TO_WGPU * perspective *
+ * look_at_rh(eye, eye + dir, +y), column-major. dir is the viewing direction, fovy in
+ * radians (the reference passes fov.to_degrees() here; pass that value to reproduce it). */
+int vox_camera_global_matrix(const float eye[3], const float dir[3], float aspect, float fovy,
+                             float znear, float zfar, float out_colmajor[16]);
+
+/* Coord3DF::to_chunk_coord (src/coordinate.rs:33-38) for chunk size n: floor(v) >> log2(n). */
+vox_chunk_coord vox_world_to_chunk(const float pos[3], int32_t chunk_size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* VOXGPU_SERVE_H */

@@ -1,0 +1,86 @@
+"""The chunk streaming engine (include/voxgpu_serve.h) on the GPU: continuous batching,
+the device mesh cache, LRU eviction under a byte budget, latency statistics, and the
+invariance of every chunk's mesh under batching (alone == in the mix)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from gpu_util import torch_cuda
+
+pytestmark = pytest.mark.gpu
+
+
+def run_frames(vox, server, frames, dt=1.0 / 60):
+    for k in range(frames):
+        eye, d = vox.serving_camera(k * dt)
+        m = vox.camera_matrix(eye, d, zfar=500.0)
+        server.frame(m, eye)
+    server.drain()
+
+
+class _DeviceBytes:
+    """A raw device pointer seen through the CUDA array interface (a torch view)."""
+
+    def __init__(self, ptr, n):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "|u1", "data": (ptr, True),
+                                         "version": 2}
+
+
+def fetch(ptr, nbytes):
+    """Copies nbytes from a raw device pointer to host memory."""
+    torch = torch_cuda()
+    torch.cuda.synchronize()
+    if nbytes == 0:
+        return np.zeros(0, np.uint8)
+    return torch.as_tensor(_DeviceBytes(ptr, nbytes), device="cuda").cpu().numpy()
+
+
+def test_camera_and_world_to_chunk(vox):
+    c = vox.lib().vox_world_to_chunk((ctypes.c_float * 3)(-0.5, 15.9, 16.0), 16)
+    assert (c.x, c.y, c.z) == (-1, 0, 1)
+    m = np.array(vox.camera_matrix((0, 0, 0), (0, 0, -1)), np.float32)
+    assert np.isfinite(m).all()
+
+
+def test_serving_meshes_equal_alone_and_complete(vox, oracle):
+    wl = vox.workload("heightmap")
+    cfg = wl.config()
+    server = vox.Server(cfg, view_radius=12, max_batch=32, slots=3)
+    run_frames(vox, server, 90)
+    st = server.stats()
+    assert st.requested > 100
+    assert st.completed == st.requested and st.pending == 0
+    assert 0 < st.latency_p50_ms <= st.latency_p99_ms <= st.latency_max_ms
+    # every resident chunk's mesh equals the chunk meshed alone with all lateral
+    # neighbours present, on the GPU and in the oracle
+    eye, _ = vox.serving_camera(90 / 60)
+    centre = vox.lib().vox_world_to_chunk((ctypes.c_float * 3)(*eye), 16)
+    checked = 0
+    for dz in range(-12, 13, 3):
+        for dx in range(-12, 13, 3):
+            c = (centre.x + dx, 0, centre.z + dz)
+            got = server.lookup(c)
+            if got is None:
+                continue
+            p0, p1, faces = got
+            w0, w1, woffs = oracle.gen_mesh_batch(cfg, [c], [0x0F])
+            assert faces == int(woffs[-1])
+            assert np.array_equal(fetch(p0, faces * 96), w0)
+            assert np.array_equal(fetch(p1, faces * 24), w1)
+            checked += 1
+    assert checked >= 5
+    server.close()
+
+
+def test_serving_evicts_lru_under_budget(vox):
+    wl = vox.workload("heightmap")
+    cfg = wl.config()
+    budget = 24 << 20
+    server = vox.Server(cfg, view_radius=12, max_batch=16, slots=2, cache_budget_bytes=budget)
+    run_frames(vox, server, 240)
+    st = server.stats()
+    assert st.evicted > 0
+    assert st.cache_bytes <= budget
+    assert st.completed >= st.requested - st.pending
+    server.close()

@@ -70,6 +70,25 @@ class Tuning(ctypes.Structure):
                 "ctas_per_sm": self.ctas_per_sm}
 
 
+class ServeConfig(ctypes.Structure):
+    _fields_ = [("chunk", Config), ("view_radius", ctypes.c_int32), ("y_min", ctypes.c_int32),
+                ("y_max", ctypes.c_int32), ("max_batch", ctypes.c_int32),
+                ("slots", ctypes.c_int32), ("cache_budget_bytes", ctypes.c_uint64)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [("frames", ctypes.c_uint64), ("requested", ctypes.c_uint64),
+                ("completed", ctypes.c_uint64), ("evicted", ctypes.c_uint64),
+                ("launches", ctypes.c_uint64), ("faces_resident", ctypes.c_uint64),
+                ("cache_bytes", ctypes.c_uint64), ("resident", ctypes.c_uint64),
+                ("pending", ctypes.c_uint64), ("latency_p50_ms", ctypes.c_double),
+                ("latency_p99_ms", ctypes.c_double), ("latency_max_ms", ctypes.c_double),
+                ("busy_s", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class VoxError(RuntimeError):
     def __init__(self, status: int, what: str, detail: str = ""):
         self.status = status
@@ -113,6 +132,17 @@ _SIGS = {
     "vox_autotune": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, ctypes.c_int64, _P, _P,
                                     ctypes.c_uint64, _P, ctypes.c_int32, ctypes.POINTER(Tuning)]),
     "vox_selftest_lookback_timeout": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "vox_serve_create": (ctypes.c_int, [ctypes.POINTER(ServeConfig), ctypes.POINTER(_P)]),
+    "vox_serve_destroy": (ctypes.c_int, [_P]),
+    "vox_serve_now": (ctypes.c_double, []),
+    "vox_serve_frame": (ctypes.c_int, [_P, _P, _P, ctypes.c_double]),
+    "vox_serve_drain": (ctypes.c_int, [_P]),
+    "vox_serve_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(ServeStats)]),
+    "vox_serve_lookup": (ctypes.c_int, [_P, ChunkCoord, ctypes.POINTER(_P), ctypes.POINTER(_P),
+                                        ctypes.POINTER(ctypes.c_uint64)]),
+    "vox_camera_global_matrix": (ctypes.c_int, [_P, _P, ctypes.c_float, ctypes.c_float,
+                                                ctypes.c_float, ctypes.c_float, _P]),
+    "vox_world_to_chunk": (ChunkCoord, [_P, ctypes.c_int32]),
     "vox_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_P)]),
     "vox_host_free": (ctypes.c_int, [_P]),
 }
@@ -300,6 +330,87 @@ class Context:
         p = (ctypes.c_float * 24)(*[float(v) for v in planes])
         self._check(self._lib.vox_frustum_cull(self._h, ctypes.addressof(p), _ptr(d_coords), n,
                                                _ptr(d_visible)), "vox_frustum_cull")
+
+
+def camera_matrix(eye, direction, aspect=16 / 9, fovy=1.0471976, znear=0.1, zfar=1000.0):
+    """Camera::update_global_matrix (src/camera.rs:41-51), column-major 16 floats."""
+    e = (ctypes.c_float * 3)(*eye)
+    d = (ctypes.c_float * 3)(*direction)
+    out = (ctypes.c_float * 16)()
+    st = lib().vox_camera_global_matrix(ctypes.addressof(e), ctypes.addressof(d), aspect, fovy,
+                                        znear, zfar, ctypes.addressof(out))
+    if st != VOX_OK:
+        raise VoxError(st, "vox_camera_global_matrix")
+    return list(out)
+
+
+class Server:
+    """The chunk streaming engine (include/voxgpu_serve.h)."""
+
+    def __init__(self, chunk_cfg: Config, view_radius=24, y_min=0, y_max=0, max_batch=64,
+                 slots=3, cache_budget_bytes=24 << 30):
+        self._lib = lib()
+        self.cfg = ServeConfig(chunk_cfg, view_radius, y_min, y_max, max_batch, slots,
+                               cache_budget_bytes)
+        h = _P()
+        st = self._lib.vox_serve_create(ctypes.byref(self.cfg), ctypes.byref(h))
+        if st != VOX_OK:
+            raise VoxError(st, "vox_serve_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.vox_serve_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def now() -> float:
+        return lib().vox_serve_now()
+
+    def frame(self, view_proj, eye, now=-1.0):
+        m = (ctypes.c_float * 16)(*[float(v) for v in view_proj])
+        e = (ctypes.c_float * 3)(*[float(v) for v in eye])
+        st = self._lib.vox_serve_frame(self._h, ctypes.addressof(m), ctypes.addressof(e), now)
+        if st != VOX_OK:
+            raise VoxError(st, "vox_serve_frame")
+
+    def drain(self):
+        st = self._lib.vox_serve_drain(self._h)
+        if st != VOX_OK:
+            raise VoxError(st, "vox_serve_drain")
+
+    def stats(self) -> ServeStats:
+        s = ServeStats()
+        st = self._lib.vox_serve_get_stats(self._h, ctypes.byref(s))
+        if st != VOX_OK:
+            raise VoxError(st, "vox_serve_get_stats")
+        return s
+
+    def lookup(self, coord):
+        """(device ptr out0, device ptr out1, faces) of a resident chunk, or None."""
+        p0, p1, f = _P(), _P(), ctypes.c_uint64()
+        st = self._lib.vox_serve_lookup(self._h, ChunkCoord(*coord), ctypes.byref(p0),
+                                        ctypes.byref(p1), ctypes.byref(f))
+        if st != VOX_OK:
+            return None
+        return int(p0.value or 0), int(p1.value or 0), int(f.value)
+
+
+def serving_camera(t, speed=20.0, yaw_rate=90.0, height=60.0, pitch_deg=-20.0):
+    """The simulated camera of the serving workload at time t (seconds): a straight line
+    along +x at `speed` units/s with a yaw sweep of `yaw_rate` degrees/s."""
+    import math
+    eye = (speed * t, height, 0.0)
+    yaw = math.radians(270.0 + yaw_rate * t)  # the reference camera starts at yaw 270
+    pitch = math.radians(pitch_deg)
+    d = (math.cos(yaw) * math.cos(pitch), math.sin(pitch), math.sin(yaw) * math.cos(pitch))
+    return eye, d
 
 
 def grid_coords(xs, ys, zs):

@@ -21,6 +21,7 @@ PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 SRC_ROOT = os.path.dirname(PKG_DIR)                       # wgpu-voxel-engine_gb300/
 REPO = os.path.dirname(SRC_ROOT)
 CSRC = os.path.join(SRC_ROOT, "csrc")
+HOST = os.path.join(SRC_ROOT, "host")
 INCLUDE = os.path.join(REPO, "include")
 MACHINE = platform.machine()
 BUILD_DIR = os.path.join(SRC_ROOT, "_build", MACHINE)
@@ -72,10 +73,11 @@ def build_library(verbose: bool = False, extra_nvcc=None) -> str:
     nvcc = os.path.join(cuda, "bin", "nvcc")
     os.makedirs(BUILD_DIR, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
-    headers.append(os.path.join(INCLUDE, "voxgpu.h"))
+    headers += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
     hdr_time = _newest(headers)
     cu = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
     cpp = sorted(f for f in os.listdir(CSRC) if f.endswith(".cpp"))
+    host = sorted(f for f in os.listdir(HOST) if f.endswith(".cpp")) if os.path.isdir(HOST) else []
     nv_flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false",
                        "-Xcompiler", "-fPIC,-ffp-contract=off",
                        "-I", INCLUDE, "-I", CSRC] + list(extra_nvcc or [])
@@ -84,8 +86,8 @@ def build_library(verbose: bool = False, extra_nvcc=None) -> str:
                  "-I", INCLUDE, "-I", CSRC, "-I", os.path.join(cuda, "include")]
     jobs = []
     objs = []
-    for f in cu + cpp:
-        src = os.path.join(CSRC, f)
+    for f in cu + cpp + host:
+        src = os.path.join(HOST if f in host else CSRC, f)
         obj = os.path.join(BUILD_DIR, f + ".o")
         objs.append(obj)
         if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(src), hdr_time):
