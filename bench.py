@@ -51,7 +51,8 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--workload", choices=list(WORKLOAD_TEXT) + ["serving"], default="heightmap")
     p.add_argument("--layout", choices=["vertex", "instanced"], default="vertex")
-    p.add_argument("--slab", type=int, default=512, help="chunks per launch (stress workload)")
+    p.add_argument("--slab", type=int, default=1024,
+                   help="chunks per launch (stress workload; 1024 x 48 MB of output per launch)")
     p.add_argument("--cpu-seconds", type=float, default=8.0,
                    help="wall time of the CPU-baseline sample")
     p.add_argument("--e2e-steps", type=int, default=50)
@@ -464,8 +465,8 @@ def e2e_host(ctx, wl, masks, n, total_faces, b0, b1, args, np):
             "api": "vox_gen_mesh_host (pinned host buffers, synchronous)"}
 
 
-def serving_run(frames: int, paced: bool, view_radius: int = 24, slots: int = 3,
-                max_batch: int = 64):
+def serving_run(frames: int, paced: bool, view_radius: int = 24, slots: int = 4,
+                max_batch: int = 256):
     """The serving workload: the simulated camera (20 units/s along +x, 90 deg/s yaw
     sweep, 60 frames/s) drives the streaming engine over the heightmap terrain (16^3
     chunks, view radius 24 chunks, 24 GB device cache with LRU eviction). Paced: frame k

@@ -23,7 +23,7 @@ class _DeviceBytes:
     """A raw device pointer seen through the CUDA array interface (a torch view)."""
 
     def __init__(self, ptr, n):
-        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "|u1", "data": (ptr, True),
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "|u1", "data": (ptr, False),
                                          "version": 2}
 
 

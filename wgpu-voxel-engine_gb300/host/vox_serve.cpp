@@ -63,7 +63,9 @@ struct Entry {
 struct Slot {
   vox_ctx* ctx = nullptr;
   cudaStream_t stream = nullptr;
-  cudaEvent_t done = nullptr;
+  cudaEvent_t start = nullptr;  // recorded before the batch's first copy
+  cudaEvent_t done = nullptr;   // recorded after its offsets reach the host
+  double launched_at = 0.0;     // engine clock when `start` was recorded
   bool busy = false;
   vox_chunk_coord* d_coords = nullptr;
   uint8_t* d_mask = nullptr;
@@ -131,14 +133,20 @@ void release(vox_serve* s, Entry& e) {
   s->stats.faces_resident -= e.faces;
 }
 
-// Evicts least-recently-seen resident chunks that were not seen this frame until
-// `need` more bytes fit in the budget; returns false if that is impossible.
+// Evicts least-recently-seen resident chunks until `need` more bytes fit in the budget:
+// first those not seen this frame, then (when the visible set alone exceeds the budget)
+// visible ones. Returns false if the budget cannot hold `need` at all.
 bool make_room(vox_serve* s, uint64_t need) {
+  if (need > s->cfg.cache_budget_bytes) return false;
   while (s->stats.cache_bytes + need > s->cfg.cache_budget_bytes) {
     auto victim = s->entries.end();
-    for (auto it = s->entries.begin(); it != s->entries.end(); ++it) {
-      if (it->second.state != Entry::RESIDENT || it->second.last_seen >= s->frame) continue;
-      if (victim == s->entries.end() || it->second.last_seen < victim->second.last_seen) victim = it;
+    for (int pass = 0; pass < 2 && victim == s->entries.end(); ++pass) {
+      for (auto it = s->entries.begin(); it != s->entries.end(); ++it) {
+        if (it->second.state != Entry::RESIDENT) continue;
+        if (pass == 0 && it->second.last_seen >= s->frame) continue;
+        if (victim == s->entries.end() || it->second.last_seen < victim->second.last_seen)
+          victim = it;
+      }
     }
     if (victim == s->entries.end()) return false;
     release(s, victim->second);
@@ -166,6 +174,8 @@ int launch_batch(vox_serve* s, Slot& sl, std::vector<vox_chunk_coord>&& chunks) 
   }
   s->stats.cache_bytes += bytes;
   std::vector<uint8_t> masks(m, s->cfg.chunk.cull_mode == VOX_CULL_FULL6 ? 0x3F : 0x0F);
+  sl.launched_at = mono_now();
+  cudaEventRecord(sl.start, sl.stream);
   cudaMemcpyAsync(sl.d_coords, chunks.data(), sizeof(vox_chunk_coord) * m, cudaMemcpyHostToDevice,
                   sl.stream);
   cudaMemcpyAsync(sl.d_mask, masks.data(), (size_t)m, cudaMemcpyHostToDevice, sl.stream);
@@ -233,7 +243,14 @@ int poll_and_admit(vox_serve* s, bool wait) {
     cudaError_t q = wait ? cudaEventSynchronize(sl.done) : cudaEventQuery(sl.done);
     if (q == cudaErrorNotReady) continue;
     if (q != cudaSuccess) return VOX_ERR_CUDA;
-    const int st = integrate(s, sl, mono_now());
+    // Completion time from the GPU's own timestamps (the slot's stream is idle when a
+    // batch is admitted, so `start` fires as the batch is enqueued), not from when the
+    // host happened to poll.
+    float ms = 0.0f;
+    const double t_done = cudaEventElapsedTime(&ms, sl.start, sl.done) == cudaSuccess
+                              ? sl.launched_at + (double)ms * 1e-3
+                              : mono_now();
+    const int st = integrate(s, sl, t_done);
     if (st != VOX_OK) return st;
   }
   // admit: nearest requests first
@@ -243,9 +260,13 @@ int poll_and_admit(vox_serve* s, bool wait) {
                 return dist2(s, a) < dist2(s, b);
               });
     size_t head = 0;
+    // a batch reserves est_faces_per_chunk faces per chunk; keep one batch within the budget
+    const uint64_t per_chunk = s->est_faces_per_chunk * s->bytes_per_face;
+    const size_t fit = (size_t)std::max<uint64_t>(1, s->cfg.cache_budget_bytes / per_chunk);
     for (Slot& sl : s->slots) {
       if (sl.busy || head >= s->queue.size()) continue;
-      const size_t take = std::min<size_t>((size_t)s->cfg.max_batch, s->queue.size() - head);
+      const size_t take =
+          std::min<size_t>(std::min<size_t>((size_t)s->cfg.max_batch, fit), s->queue.size() - head);
       std::vector<vox_chunk_coord> chunks(s->queue.begin() + head, s->queue.begin() + head + take);
       const int st = launch_batch(s, sl, std::move(chunks));
       if (st == VOX_ERR_OOM) break;  // the cache is full of visible chunks: retry later
@@ -309,7 +330,7 @@ int vox_serve_create(const vox_serve_config* cfg, vox_serve** out) {
   s->slots.resize(cfg->slots);
   for (Slot& sl : s->slots) {
     if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess)
+        cudaEventCreate(&sl.start) != cudaSuccess || cudaEventCreate(&sl.done) != cudaSuccess)
       return VOX_ERR_CUDA;
     if ((st = vox_ctx_create(&cfg->chunk, sl.stream, &sl.ctx)) != VOX_OK) return st;
     if (cudaMalloc(&sl.d_coords, sizeof(vox_chunk_coord) * cfg->max_batch) != cudaSuccess ||
@@ -340,6 +361,7 @@ int vox_serve_destroy(vox_serve* s) {
     cudaFree(sl.d_offsets);
     if (sl.h_offsets) cudaFreeHost(sl.h_offsets);
     if (sl.done) cudaEventDestroy(sl.done);
+    if (sl.start) cudaEventDestroy(sl.start);
     if (sl.stream) cudaStreamDestroy(sl.stream);
   }
   vox_ctx_destroy(s->cull_ctx);
@@ -400,6 +422,10 @@ int vox_serve_drain(vox_serve* s) {
     if (!busy && s->queue.empty()) return VOX_OK;
     const int st = poll_and_admit(s, true);
     if (st != VOX_OK) return st;
+    bool launched = false;
+    for (Slot& sl : s->slots) launched = launched || sl.busy;
+    // nothing in flight and nothing admitted: the budget cannot hold the next batch
+    if (!launched && !s->queue.empty()) return VOX_ERR_OOM;
   }
 }
 
