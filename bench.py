@@ -60,7 +60,8 @@ def parse_args():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--tuning", default=None,
-                   help="force a launch shape 'threads,stage_faces,ctas_per_sm' (no autotune)")
+                   help="force a launch shape 'threads,stage_faces,ctas_per_sm[,schedule]' "
+                        "(schedule 0 look-back, 1 phased; no autotune)")
     p.add_argument("--frames", type=int, default=10000, help="serving workload: frames")
     p.add_argument("--paced", action="store_true", help="serving workload: real-time 60 fps")
     p.add_argument("--latency-frames", type=int, default=300,
@@ -273,8 +274,7 @@ def run_ours(args):
     # launch shape from the autotuner, timed on the first slab (setup, not timed)
     tuning = None
     if args.tuning:
-        th, st, cps = (int(v) for v in args.tuning.split(","))
-        ctx.set_tuning(th, st, cps)
+        ctx.set_tuning(*(int(v) for v in args.tuning.split(",")))
     elif not args.no_autotune:
         a, b = slabs[0]
         with torch.cuda.stream(stream):

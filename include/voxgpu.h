@@ -225,17 +225,26 @@ typedef struct vox_tuning {
   int32_t threads;     /* CTA size; each chunk size has two (8: 32/64, 16: 128/256,
                           32: 256/512, 64: 512/1024) */
   int32_t stage_faces; /* 0: every lane stores its face records straight to global memory;
-                          32: each warp stages 32 faces at a time in shared memory and
-                          sends them with a TMA bulk copy */
+                          32: each warp stages 32 faces at a time in one shared-memory
+                          buffer and sends them with a TMA bulk copy; 64: the same with
+                          two buffers per warp (one fills while the other is sent) */
   int32_t ctas_per_sm; /* resident CTAs per SM of the persistent grid; 0 = as many as fit */
-  int32_t reserved;
+  int32_t schedule;    /* VOX_SCHEDULE_LOOKBACK or VOX_SCHEDULE_PHASED */
 } vox_tuning;
+
+/* Schedules of the fused batch kernel (both write the same bytes):
+ * LOOKBACK: one pass; each chunk's output offset comes from a decoupled look-back over
+ *   its predecessors' face counts.
+ * PHASED: a cooperative launch in three phases: generate and count every chunk (the
+ *   occupancy is kept in a context-owned scratch), scan the counts once, then emit every
+ *   chunk at its known offset. No chunk waits for another inside a phase. */
+enum { VOX_SCHEDULE_LOOKBACK = 0, VOX_SCHEDULE_PHASED = 1 };
 
 int vox_ctx_get_tuning(vox_ctx* ctx, vox_tuning* out);
 int vox_ctx_set_tuning(vox_ctx* ctx, const vox_tuning* tuning);
 
-/* Autotuner: times every candidate launch shape (CTA size x staging window x CTAs per SM)
- * on the given batch with vox_gen_mesh_batch (same arguments; iters launches each),
+/* Autotuner: times every candidate launch shape (schedule x CTA size x staging window x
+ * CTAs per SM) on the given batch with vox_gen_mesh_batch (same arguments; iters launches each),
  * keeps the fastest in the context and returns it in *out. The outputs of every
  * candidate are identical; the buffers hold the last run's result. */
 int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,

@@ -38,9 +38,18 @@ def to_np(t, nbytes=None):
     return a
 
 
-def gpu_gen_mesh(vox, cfg, coords, masks=None, index_base=0, cap=None, expect_status=None):
+def use_schedule(ctx, schedule):
+    """Keeps the context's launch shape and selects a schedule (None: leave it)."""
+    if schedule is not None:
+        t = ctx.tuning()
+        ctx.set_tuning(t.threads, t.stage_faces, t.ctas_per_sm, schedule)
+
+
+def gpu_gen_mesh(vox, cfg, coords, masks=None, index_base=0, cap=None, expect_status=None,
+                 schedule=None):
     """Runs vox_gen_mesh_batch; returns (out0 bytes, out1 bytes, offsets, status)."""
     ctx = ctx_for(vox, cfg)
+    use_schedule(ctx, schedule)
     n = len(coords)
     d_coords = to_dev(np.asarray(coords, np.int32).reshape(-1, 3))
     d_mask = None if masks is None else to_dev(np.asarray(masks, np.uint8))

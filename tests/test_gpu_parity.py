@@ -6,11 +6,12 @@ instance records must equal the oracle's on the same inputs (signed zeros includ
 import numpy as np
 import pytest
 
-from gpu_util import ctx_for, dev_bytes, gpu_gen_mesh, gpu_generate, to_dev, to_np
+from gpu_util import ctx_for, dev_bytes, gpu_gen_mesh, gpu_generate, to_dev, to_np, use_schedule
 
 pytestmark = pytest.mark.gpu
 
 LAYOUTS = [0, 1]  # vertex, instanced
+SCHEDULES = [0, 1]  # look-back, phased (cooperative launch)
 
 
 def small_coords():
@@ -129,7 +130,8 @@ def test_mesh_single_matches_oracle(vox, oracle, n, layout, cull):
 
 @pytest.mark.parametrize("n", [16, 32])
 @pytest.mark.parametrize("layout", LAYOUTS)
-def test_mesh_batch_pool_matches_oracle(vox, oracle, n, layout):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_mesh_batch_pool_matches_oracle(vox, oracle, n, layout, schedule):
     rng = np.random.default_rng(7 + n + layout)
     cfg = vox.make_config(chunk_size=n, layout=layout)
     slots = 9
@@ -141,6 +143,7 @@ def test_mesh_batch_pool_matches_oracle(vox, oracle, n, layout):
     nbr = rng.integers(-1, slots, (m, 6)).astype(np.int32)
     coords = [(int(a), 0, int(b)) for a, b in rng.integers(-20, 20, (m, 2))]
     ctx = ctx_for(vox, cfg)
+    use_schedule(ctx, schedule)
     b0, b1 = ctx.sizes.bytes_per_face_out0, ctx.sizes.bytes_per_face_out1
     cap = ctx.sizes.max_faces_per_chunk * m
     o0, o1 = dev_bytes(cap * b0), dev_bytes(cap * b1)
@@ -165,10 +168,11 @@ def test_mesh_batch_pool_matches_oracle(vox, oracle, n, layout):
     ctx.close()
 
 
-def compare_batch(vox, oracle, cfg, coords, masks, index_base=0):
+def compare_batch(vox, oracle, cfg, coords, masks, index_base=0, schedule=None):
     w0, w1, woffs = oracle.gen_mesh_batch(cfg, coords, masks, index_base)
     total = int(woffs[-1])
-    g0, g1, goffs, _ = gpu_gen_mesh(vox, cfg, coords, masks, index_base, cap=max(total, 1))
+    g0, g1, goffs, _ = gpu_gen_mesh(vox, cfg, coords, masks, index_base, cap=max(total, 1),
+                                    schedule=schedule)
     assert np.array_equal(goffs, woffs)
     assert np.array_equal(g0, w0)
     assert np.array_equal(g1, w1)
@@ -176,41 +180,49 @@ def compare_batch(vox, oracle, cfg, coords, masks, index_base=0):
 
 
 @pytest.mark.parametrize("layout", LAYOUTS)
-def test_plain_workload_full(vox, oracle, layout):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_plain_workload_full(vox, oracle, layout, schedule):
     """8x8 chunks of 32^3 around the origin, 2-D Perlin heightmap (the CPU-runnable case)."""
     wl = vox.workload("plain")
-    total = compare_batch(vox, oracle, wl.config(layout=layout), wl.coords, wl.masks())
+    total = compare_batch(vox, oracle, wl.config(layout=layout), wl.coords, wl.masks(),
+                          schedule=schedule)
     assert total > 0
 
 
 @pytest.mark.parametrize("layout", LAYOUTS)
-def test_heightmap_workload_full(vox, oracle, layout):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_heightmap_workload_full(vox, oracle, layout, schedule):
     """32x32 chunks of 16^3, 2-D fBm: all-air, all-solid and surface chunks."""
     wl = vox.workload("heightmap")
-    total = compare_batch(vox, oracle, wl.config(layout=layout), wl.coords, wl.masks())
+    total = compare_batch(vox, oracle, wl.config(layout=layout), wl.coords, wl.masks(),
+                          schedule=schedule)
     assert total > 0
 
 
 @pytest.mark.parametrize("cull", [0, 1])
-def test_density_workload_slab(vox, oracle, cull):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_density_workload_slab(vox, oracle, cull, schedule):
     """A 4x3x4 block of the 3-D density terrain around its surface (y = 256)."""
     wl = vox.workload("density")
     coords = vox.grid_coords(range(4, 8), range(7, 10), range(4, 8))
     total = compare_batch(vox, oracle, wl.config(cull_mode=cull), coords,
-                          vox.neighbour_masks(coords, full6=bool(cull)))
+                          vox.neighbour_masks(coords, full6=bool(cull)), schedule=schedule)
     assert total > 0
 
 
 @pytest.mark.parametrize("layout", LAYOUTS)
-def test_stress_workload_sample(vox, oracle, layout):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_stress_workload_sample(vox, oracle, layout, schedule):
     """Four isolated 64^3 Bernoulli(0.5) chunks (index base 1000)."""
     wl = vox.workload("stress")
     coords = [(i, 0, 0) for i in range(4)]
-    total = compare_batch(vox, oracle, wl.config(layout=layout), coords, None, index_base=1000)
+    total = compare_batch(vox, oracle, wl.config(layout=layout), coords, None, index_base=1000,
+                          schedule=schedule)
     assert total > 4 * 300_000
 
 
-def test_capacity_overflow_reports_and_keeps_prefix(vox, oracle):
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_capacity_overflow_reports_and_keeps_prefix(vox, oracle, schedule):
     wl = vox.workload("heightmap")
     cfg = wl.config()
     coords = wl.coords[:64]
@@ -218,7 +230,8 @@ def test_capacity_overflow_reports_and_keeps_prefix(vox, oracle):
     w0, w1, woffs = oracle.gen_mesh_batch(cfg, coords, masks)
     total = int(woffs[-1])
     cap = total // 3
-    g0, g1, goffs, st = gpu_gen_mesh(vox, cfg, coords, masks, cap=cap, expect_status=True)
+    g0, g1, goffs, st = gpu_gen_mesh(vox, cfg, coords, masks, cap=cap, expect_status=True,
+                                     schedule=schedule)
     assert st == vox.VOX_ERR_CAPACITY
     assert np.array_equal(goffs, woffs)
     assert np.array_equal(g0, w0[:cap * 96]) and np.array_equal(g1, w1[:cap * 24])
@@ -341,23 +354,27 @@ def test_every_launch_shape_is_bit_exact(vox, oracle, wlname, sub, layout):
     o0, o1 = dev_bytes(total * b0), dev_bytes(max(total * b1, 16))
     offs = to_dev(np.zeros(len(coords) + 1, np.uint64))
     tried = 0
-    for threads in threads_options(n):
-        for stage in (0, 32):
-            for cps in (0, 2):
-                try:
-                    ctx.set_tuning(threads, stage, cps)
-                except vox.VoxError:
-                    continue  # the staging window does not fit in shared memory
-                o0.fill_(0x5A)
-                ctx.gen_mesh_batch(d_coords, d_mask, len(coords), o0, o1 if b1 else None, total, offs)
-                ctx.sync()
-                tag = (threads, stage, cps)
-                assert np.array_equal(to_np(offs), woffs), tag
-                assert np.array_equal(to_np(o0, total * b0), w0), tag
-                if b1:
-                    assert np.array_equal(to_np(o1, total * b1), w1), tag
-                tried += 1
-    assert tried >= 5
+    for sched in (vox.SCHEDULE_LOOKBACK, vox.SCHEDULE_PHASED):
+        for threads in threads_options(n):
+            for stage in (0, 32, 64):
+                for cps in (0, 2):
+                    try:
+                        ctx.set_tuning(threads, stage, cps, sched)
+                    except vox.VoxError:
+                        continue  # the staging window does not fit in shared memory
+                    for rep in range(2):  # the second launch reuses the reset queues
+                        o0.fill_(0x5A)
+                        offs.fill_(0)
+                        ctx.gen_mesh_batch(d_coords, d_mask, len(coords), o0, o1 if b1 else None,
+                                           total, offs)
+                        ctx.sync()
+                        tag = (sched, threads, stage, cps, rep)
+                        assert np.array_equal(to_np(offs), woffs), tag
+                        assert np.array_equal(to_np(o0, total * b0), w0), tag
+                        if b1:
+                            assert np.array_equal(to_np(o1, total * b1), w1), tag
+                    tried += 1
+    assert tried >= 10
     ctx.close()
 
 
@@ -375,9 +392,11 @@ def test_autotune_picks_a_valid_shape(vox, oracle):
     offs = to_dev(np.zeros(len(coords) + 1, np.uint64))
     t = ctx.autotune(d_coords, d_mask, len(coords), o0, o1, total, offs, iters=2)
     assert t.threads in threads_options(16)
-    assert t.stage_faces in (0, 32)
+    assert t.stage_faces in (0, 32, 64)
     got = ctx.tuning()
-    assert (got.threads, got.stage_faces, got.ctas_per_sm) == (t.threads, t.stage_faces, t.ctas_per_sm)
+    assert t.schedule in (vox.SCHEDULE_LOOKBACK, vox.SCHEDULE_PHASED)
+    assert (got.threads, got.stage_faces, got.ctas_per_sm, got.schedule) == (
+        t.threads, t.stage_faces, t.ctas_per_sm, t.schedule)
     o0.fill_(0)
     ctx.gen_mesh_batch(d_coords, d_mask, len(coords), o0, o1, total, offs)
     ctx.sync()
@@ -407,7 +426,7 @@ def test_bounded_wait_times_out_and_context_survives(vox, oracle):
     ctx.close()
 
 
-@pytest.mark.parametrize("stage", [0, 32])
+@pytest.mark.parametrize("stage", [0, 32, 64])
 def test_single_chunk_direct_and_staged(vox, oracle, stage):
     rng = np.random.default_rng(11)
     cfg = vox.make_config(chunk_size=32)

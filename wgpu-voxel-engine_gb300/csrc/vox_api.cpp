@@ -21,7 +21,9 @@
 using namespace vox;
 
 // Faces per warp staging buffer (the kernels' kWarpBatch).
-constexpr int kWarpStageFaces = 32;
+// staging windows of a warp: one 32-face buffer (32) or two (64)
+constexpr int kStageSingle = 32;
+constexpr int kStageDouble = 64;
 
 struct vox_ctx {
   vox_config cfg{};
@@ -34,12 +36,19 @@ struct vox_ctx {
   const KernelSet* ks = nullptr;
   GenDev gen{};
   int gm = GM_HEIGHT;
-  // tuning: CTA-size option, staging window (0 = direct stores), resident CTAs per SM
+  // tuning: CTA-size option, staging window (0 = direct stores), resident CTAs per SM,
+  // schedule (look-back or phased)
   int topt = 0;
   int stage_faces = 0;
   int ctas_per_sm = 0;
+  int schedule = VOX_SCHEDULE_LOOKBACK;
   int spin_limit = kSpinLimit;
-  int batch_grid[4] = {0, 0, 0, 0};  // persistent grid per gen mode
+  int batch_grid[4] = {0, 0, 0, 0};   // persistent grid per gen mode (look-back kernel)
+  int phased_grid[4] = {0, 0, 0, 0};  // co-resident grid per gen mode (phased kernel)
+  // phased schedule: per-chunk occupancy + halo spill and face totals
+  uint32_t* d_scratch = nullptr;
+  uint32_t* d_counts = nullptr;
+  size_t scratch_cap = 0;  // chunks
   TablesDev* d_tables = nullptr;
   BatchCtl* d_ctl = nullptr;
   BatchCtl* h_ctl = nullptr;  // pinned
@@ -153,31 +162,57 @@ int prepare_kernel(vox_ctx* ctx, const void* fn, int smem) {
 }
 
 // Validates a tuning and computes the persistent grid of every generator mode for it.
-int apply_tuning(vox_ctx* ctx, int topt, int stage_faces, int ctas_per_sm) {
+int apply_tuning(vox_ctx* ctx, int topt, int stage_faces, int ctas_per_sm, int schedule) {
   const KernelSet& ks = *ctx->ks;
   const int layout = ctx->cfg.layout;
   if (topt < 0 || topt > 1) return fail(ctx, VOX_ERR_INVALID, "unsupported CTA size");
-  if (stage_faces != 0 && stage_faces != kWarpStageFaces)
-    return fail(ctx, VOX_ERR_INVALID, "stage_faces must be 0 (direct stores) or %d",
-                kWarpStageFaces);
+  if (stage_faces != 0 && stage_faces != kStageSingle && stage_faces != kStageDouble)
+    return fail(ctx, VOX_ERR_INVALID, "stage_faces must be 0 (direct stores), %d or %d",
+                kStageSingle, kStageDouble);
   if (ctas_per_sm < 0) return fail(ctx, VOX_ERR_INVALID, "ctas_per_sm must be >= 0");
+  if (schedule != VOX_SCHEDULE_LOOKBACK && schedule != VOX_SCHEDULE_PHASED)
+    return fail(ctx, VOX_ERR_INVALID, "schedule must be VOX_SCHEDULE_LOOKBACK or VOX_SCHEDULE_PHASED");
   const int smem = ks.smem_total(layout, ks.threads[topt], stage_faces);
   if (smem > ctx->max_smem_optin - 256)
     return fail(ctx, VOX_ERR_INVALID, "staging window exceeds shared memory");
-  int grid[4];
+  int grid[4], pgrid[4];
   for (int gm = 0; gm < 4; ++gm) {
-    int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-        &per_sm, ks.batch[gm][layout][topt], ks.threads[topt], smem);
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
-    if (per_sm < 1) return fail(ctx, VOX_ERR_INVALID, "kernel does not fit on an SM");
-    if (ctas_per_sm > 0) per_sm = std::min(per_sm, ctas_per_sm);
-    grid[gm] = per_sm * ctx->num_sms;
+    for (int k = 0; k < 2; ++k) {
+      // the phased kernel's grid must be co-resident (cooperative launch): its occupancy
+      // is an upper bound, never exceeded
+      const void* fn = k == 0 ? ks.batch[gm][layout][topt] : ks.phased[gm][layout][topt];
+      int per_sm = 0;
+      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, ks.threads[topt], smem);
+      if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+      if (per_sm < 1) return fail(ctx, VOX_ERR_INVALID, "kernel does not fit on an SM");
+      if (ctas_per_sm > 0) per_sm = std::min(per_sm, ctas_per_sm);
+      (k == 0 ? grid : pgrid)[gm] = per_sm * ctx->num_sms;
+    }
   }
   ctx->topt = topt;
   ctx->stage_faces = stage_faces;
   ctx->ctas_per_sm = ctas_per_sm;
-  for (int gm = 0; gm < 4; ++gm) ctx->batch_grid[gm] = grid[gm];
+  ctx->schedule = schedule;
+  for (int gm = 0; gm < 4; ++gm) {
+    ctx->batch_grid[gm] = grid[gm];
+    ctx->phased_grid[gm] = pgrid[gm];
+  }
+  return VOX_OK;
+}
+
+// Scratch of the phased schedule for n chunks (grows; never shrinks).
+int ensure_scratch(vox_ctx* ctx, size_t n) {
+  if (n <= ctx->scratch_cap) return VOX_OK;
+  const size_t cap = std::max<size_t>(n, 1024);
+  cudaFree(ctx->d_scratch);
+  cudaFree(ctx->d_counts);
+  ctx->d_scratch = nullptr;
+  ctx->d_counts = nullptr;
+  ctx->scratch_cap = 0;
+  VOX_CUDA(ctx, cudaMalloc(&ctx->d_scratch, cap * (size_t)ctx->ks->spill_bytes),
+           "cudaMalloc(scratch)");
+  VOX_CUDA(ctx, cudaMalloc(&ctx->d_counts, cap * sizeof(uint32_t)), "cudaMalloc(counts)");
+  ctx->scratch_cap = cap;
   return VOX_OK;
 }
 
@@ -215,6 +250,8 @@ MeshArgs base_args(vox_ctx* ctx) {
   a.full6 = ctx->cfg.cull_mode == VOX_CULL_FULL6 ? 1 : 0;
   a.stage_faces = ctx->stage_faces;
   a.spin_limit = ctx->spin_limit;
+  a.scratch = ctx->d_scratch;
+  a.counts = ctx->d_counts;
   return a;
 }
 
@@ -241,17 +278,32 @@ int check_outputs(vox_ctx* ctx, void* out0, void* out1, uint64_t cap) {
 }
 
 int batch_launch(vox_ctx* ctx, MeshArgs& a, int gm) {
+  const int layout = ctx->cfg.layout;
+  const int threads = ctx->ks->threads[ctx->topt];
+  const int smem = ctx->ks->smem_total(layout, threads, ctx->stage_faces);
+  if (ctx->schedule == VOX_SCHEDULE_PHASED) {
+    int st = ensure_scratch(ctx, (size_t)a.n);
+    if (st != VOX_OK) return st;
+    a.scratch = ctx->d_scratch;
+    a.counts = ctx->d_counts;
+    ++ctx->launches;
+    const void* fn = ctx->ks->phased[gm][layout][ctx->topt];
+    const int grid = std::max(1, std::min(a.n, ctx->phased_grid[gm]));
+    void* params[] = {&a};
+    VOX_CUDA(ctx, cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), params, (size_t)smem,
+                                              ctx->stream),
+             "cudaLaunchCooperativeKernel");
+    return VOX_OK;
+  }
   int st = ensure_state(ctx, (size_t)a.n);
   if (st != VOX_OK) return st;
   st = before_batch_launch(ctx);
   if (st != VOX_OK) return st;
   a.state = ctx->d_state;
-  const int layout = ctx->cfg.layout;
   const void* fn = ctx->ks->batch[gm][layout][ctx->topt];
-  const int smem = ctx->ks->smem_total(layout, ctx->ks->threads[ctx->topt], ctx->stage_faces);
   const int grid = std::max(1, std::min(a.n, ctx->batch_grid[gm]));
   void* params[] = {&a};
-  return launch(ctx, fn, grid, ctx->ks->threads[ctx->topt], smem, params);
+  return launch(ctx, fn, grid, threads, smem, params);
 }
 
 }  // namespace
@@ -346,7 +398,8 @@ int vox_ctx_create(const vox_config* cfg, void* stream, vox_ctx** out) {
   const int layout = cfg->layout;
   for (int gm = 0; gm < 4; ++gm)
     for (int t = 0; t < 2; ++t)
-      if ((st = prepare_kernel(ctx, ctx->ks->batch[gm][layout][t], ctx->max_smem_optin)) != VOX_OK)
+      if ((st = prepare_kernel(ctx, ctx->ks->batch[gm][layout][t], ctx->max_smem_optin)) != VOX_OK ||
+          (st = prepare_kernel(ctx, ctx->ks->phased[gm][layout][t], ctx->max_smem_optin)) != VOX_OK)
         return cleanup(st);
   for (int t = 0; t < 2; ++t)
     if ((st = prepare_kernel(ctx, ctx->ks->single[layout][t], ctx->max_smem_optin)) != VOX_OK)
@@ -354,7 +407,8 @@ int vox_ctx_create(const vox_config* cfg, void* stream, vox_ctx** out) {
   const int gsmem = ctx->ks->smem_total(VOX_LAYOUT_VERTEX, ctx->ks->gen_threads, 0);
   for (int gm = 1; gm < 4; ++gm)
     if ((st = prepare_kernel(ctx, ctx->ks->generate[gm], gsmem)) != VOX_OK) return cleanup(st);
-  if ((st = apply_tuning(ctx, 0, default_stage_faces(*ctx->ks, layout), 0)) != VOX_OK)
+  if ((st = apply_tuning(ctx, 0, default_stage_faces(*ctx->ks, layout), 0,
+                          VOX_SCHEDULE_LOOKBACK)) != VOX_OK)
     return cleanup(st);
   if ((st = ensure_state(ctx, 1024)) != VOX_OK) return cleanup(st);
   if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return cleanup(VOX_ERR_CUDA);
@@ -368,6 +422,8 @@ int vox_ctx_destroy(vox_ctx* ctx) {
   cudaFree(ctx->d_tables);
   cudaFree(ctx->d_ctl);
   cudaFree(ctx->d_state);
+  cudaFree(ctx->d_scratch);
+  cudaFree(ctx->d_counts);
   cudaFree(ctx->d_in);
   cudaFree(ctx->d_offsets);
   cudaFree(ctx->d_out0);
@@ -389,10 +445,19 @@ static int sync_locked(vox_ctx* ctx) {
   VOX_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
   const unsigned err = ctx->h_ctl->err;
   if (err == 0) return VOX_OK;
-  VOX_CUDA(ctx, cudaMemsetAsync(&ctx->d_ctl->err, 0, sizeof(unsigned), ctx->stream),
-           "cudaMemsetAsync(err)");
+  // Clear the error bits. After a timeout a phased launch may have left its queues and
+  // its barrier count mid-way: reset them too (the epoch and generation words stay).
+  ctx->h_ctl->err = 0;
+  if (err & ERR_TIMEOUT) {
+    ctx->h_ctl->next = 0;
+    ctx->h_ctl->next2 = 0;
+    ctx->h_ctl->bar_count = 0;
+  }
+  VOX_CUDA(ctx, cudaMemcpyAsync(ctx->d_ctl, ctx->h_ctl, sizeof(BatchCtl), cudaMemcpyHostToDevice,
+                                ctx->stream),
+           "cudaMemcpyAsync(ctl)");
   VOX_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
-  if (err & ERR_TIMEOUT) return fail(ctx, VOX_ERR_TIMEOUT, "a device-side look-back wait gave up");
+  if (err & ERR_TIMEOUT) return fail(ctx, VOX_ERR_TIMEOUT, "a device-side wait gave up");
   if (err & ERR_BAD_INPUT) return fail(ctx, VOX_ERR_INVALID, "a slot index was out of range");
   return fail(ctx, VOX_ERR_CAPACITY, "output capacity exceeded");
 }
@@ -625,7 +690,7 @@ int vox_ctx_get_tuning(vox_ctx* ctx, vox_tuning* out) {
   out->threads = ctx->ks->threads[ctx->topt];
   out->stage_faces = ctx->stage_faces;
   out->ctas_per_sm = ctx->ctas_per_sm;
-  out->reserved = 0;
+  out->schedule = ctx->schedule;
   return VOX_OK;
 }
 
@@ -637,7 +702,7 @@ int vox_ctx_set_tuning(vox_ctx* ctx, const vox_tuning* t) {
     if (ctx->ks->threads[k] == t->threads) topt = k;
   if (topt < 0) return fail(ctx, VOX_ERR_INVALID, "threads must be %d or %d", ctx->ks->threads[0],
                             ctx->ks->threads[1]);
-  return apply_tuning(ctx, topt, t->stage_faces, t->ctas_per_sm);
+  return apply_tuning(ctx, topt, t->stage_faces, t->ctas_per_sm, t->schedule);
 }
 
 int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
@@ -651,14 +716,15 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
   if (st != VOX_OK) return st;
   const int N = ctx->cfg.chunk_size;
   (void)N;
-  const int stages[] = {0, kWarpStageFaces};
+  const int stages[] = {0, kStageSingle, kStageDouble};
   const int ctas[] = {0, 4, 2};
   cudaEvent_t e0, e1;
   VOX_CUDA(ctx, cudaEventCreate(&e0), "cudaEventCreate");
   VOX_CUDA(ctx, cudaEventCreate(&e1), "cudaEventCreate");
-  const int keep_t = ctx->topt, keep_s = ctx->stage_faces, keep_c = ctx->ctas_per_sm;
+  const int keep_t = ctx->topt, keep_s = ctx->stage_faces, keep_c = ctx->ctas_per_sm,
+            keep_p = ctx->schedule;
   float best_ms = 1e30f;
-  int best_t = keep_t, best_s = keep_s, best_c = keep_c;
+  int best_t = keep_t, best_s = keep_s, best_c = keep_c, best_p = keep_p;
   auto run = [&]() {
     MeshArgs a = base_args(ctx);
     a.n = n;
@@ -671,44 +737,53 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
     a.face_offsets = reinterpret_cast<unsigned long long*>(d_face_offsets);
     return batch_launch(ctx, a, ctx->gm);
   };
-  for (int t = 0; t < 2 && st == VOX_OK; ++t)
-    for (int s : stages) {
-      int full_grid = 0;
-      for (int c : ctas) {
-        if (apply_tuning(ctx, t, s, c) != VOX_OK) continue;
-        if (c == 0) full_grid = ctx->batch_grid[ctx->gm];
-        else if (ctx->batch_grid[ctx->gm] >= full_grid) continue;  // same grid as c = 0
-        if ((st = run()) != VOX_OK) break;
-        cudaEventRecord(e0, ctx->stream);
-        for (int k = 0; k < iters && st == VOX_OK; ++k) st = run();
-        cudaEventRecord(e1, ctx->stream);
-        if (st != VOX_OK) break;
-        if (cudaEventSynchronize(e1) != cudaSuccess) {
-          st = cuda_fail(ctx, cudaGetLastError(), "autotune");
-          break;
-        }
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best_ms) {
-          best_ms = ms;
-          best_t = t;
-          best_s = s;
-          best_c = c;
-        }
-      }
+  auto time_candidate = [&](int p, int t, int s, int c) -> bool {  // false: stop (error)
+    if ((st = run()) != VOX_OK) return false;
+    cudaEventRecord(e0, ctx->stream);
+    for (int k = 0; k < iters && st == VOX_OK; ++k) st = run();
+    cudaEventRecord(e1, ctx->stream);
+    if (st != VOX_OK) return false;
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      st = cuda_fail(ctx, cudaGetLastError(), "autotune");
+      return false;
     }
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_t = t;
+      best_s = s;
+      best_c = c;
+      best_p = p;
+    }
+    return true;
+  };
+  bool go = true;
+  for (int p = 0; p < 2 && go; ++p)
+    for (int t = 0; t < 2 && go; ++t)
+      for (int s : stages) {
+        int full_grid = 0;
+        for (int c : ctas) {
+          if (apply_tuning(ctx, t, s, c, p) != VOX_OK) continue;
+          const int g = p == VOX_SCHEDULE_PHASED ? ctx->phased_grid[ctx->gm] : ctx->batch_grid[ctx->gm];
+          if (c == 0) full_grid = g;
+          else if (g >= full_grid) continue;  // same grid as c = 0
+          if (!(go = time_candidate(p, t, s, c))) break;
+        }
+        if (!go) break;
+      }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   ctx->last_error.clear();
-  const int st2 = apply_tuning(ctx, best_t, best_s, best_c);
+  const int st2 = apply_tuning(ctx, best_t, best_s, best_c, best_p);
   if (st == VOX_OK) st = st2;
   if (st == VOX_OK) st = sync_locked(ctx);
-  if (st != VOX_OK) apply_tuning(ctx, keep_t, keep_s, keep_c);
+  if (st != VOX_OK) apply_tuning(ctx, keep_t, keep_s, keep_c, keep_p);
   if (out) {
     out->threads = ctx->ks->threads[ctx->topt];
     out->stage_faces = ctx->stage_faces;
     out->ctas_per_sm = ctx->ctas_per_sm;
-    out->reserved = 0;
+    out->schedule = ctx->schedule;
   }
   return st;
 }

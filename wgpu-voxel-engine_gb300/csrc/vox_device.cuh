@@ -36,6 +36,10 @@ struct Shape {
   // CTA sizes the kernels are instantiated for (rows split evenly over the threads)
   static constexpr int T0 = N == 8 ? 32 : (N == 16 ? 128 : (N == 32 ? 256 : 512));
   static constexpr int T1 = 2 * T0;
+  static constexpr int LOG2N = N == 8 ? 3 : (N == 16 ? 4 : (N == 32 ? 5 : 6));
+  // Capacity of the face-voxel list (voxels with at least one face, as (row << LOG2N) | x
+  // in 16 bits); a chunk with more face voxels is emitted row by row instead.
+  static constexpr int VCap = N > 32 ? 0 : (N * N * N < 8192 ? N * N * N : 8192);
 };
 
 __host__ __device__ constexpr int align16(int b) { return (b + 15) & ~15; }
@@ -74,8 +78,9 @@ struct SmemPlan {
   static constexpr int kHalo = align16(6 * N * (int)sizeof(RowT));
   static constexpr int kRows = align16((Shape<N>::R + 1) * 4);
   static constexpr int kNz = align16(Shape<N>::R * 2);
+  static constexpr int kVList = align16(Shape<N>::VCap * 2);
   static constexpr int kMisc = 64;
-  static constexpr int kFixed0 = kTables + kOcc + kHalo + kRows + kNz + kMisc;
+  static constexpr int kFixed0 = kTables + kOcc + kHalo + kRows + kNz + kVList + kMisc;
   // per-warp face lists (face-parallel emission)
   __host__ __device__ static int list_bytes(int threads) { return (threads / 32) * kWarpFaces * 4; }
   __host__ __device__ static int fixed(int threads) { return kFixed0 + list_bytes(threads); }
@@ -83,12 +88,13 @@ struct SmemPlan {
   static constexpr int kColK = align16((N + 2) * (N + 2) * 4);
   static constexpr int kAxisHalf = kOctGroup * align16((N + 2) * 16);
   static constexpr int kAxis = 2 * kAxisHalf;
-  static constexpr int kZRange = align16(2 * N * 4);
-  static constexpr int kGenScratch = kColK + kAxis + kZRange;
-  // staging area: two buffers per warp when staging (stage_faces > 0), else only the
-  // generation scratch
+  static constexpr int kGenScratch = kColK + kAxis;
+  // staging area: stage_faces / kWarpBatch buffers per warp when staging (stage_faces
+  // 32 or 64), else only the generation scratch
   __host__ __device__ static int stage_bytes(int threads, int stage_faces) {
-    const int b = stage_faces > 0 ? (threads / 32) * 2 * warp_buf_bytes<LAYOUT>() : 0;
+    const int b = stage_faces > 0
+                      ? (threads / 32) * (stage_faces / kWarpBatch) * warp_buf_bytes<LAYOUT>()
+                      : 0;
     return b < kGenScratch ? kGenScratch : b;
   }
   __host__ __device__ static int total(int threads, int stage_faces) {
@@ -237,15 +243,14 @@ struct ChunkSmem {
   RowT* halo;       // [6][N]: 0 -x (bits z, by y), 1 +x, 2 -z (bits x, by y), 3 +z, 4 -y (bits x, by z), 5 +y
   uint32_t* rows;   // [R + 1] exclusive face offsets per row
   uint16_t* nz;     // rows that have faces, ascending
-  int* misc;        // [0] rows with faces; [1..3] current window (k1, f0, nf)
+  uint16_t* vlist;  // face voxels in emission order, (row << LOG2N) | x (Shape<N>::VCap)
+  int* misc;        // [0] rows with faces; [1] face voxels listed in vlist, or -1
   uint32_t* lists;  // per-warp face lists (packed x, y, z, dir)
   unsigned char* stage;
   // generation scratch (aliased with the staging window)
   int* colk;        // heightmap column thresholds
   AxisX* ax;        // per-octave x-axis lattice data, [kOctGroup][N + 2]
   AxisZ* az;        // per-octave z-axis lattice data, [kOctGroup][N + 2]
-  int* zmin;        // per z: min / max column threshold over x
-  int* zmax;
 
   __device__ void carve(unsigned char* base) {
     using P = SmemPlan<N, LAYOUT>;
@@ -260,6 +265,8 @@ struct ChunkSmem {
     q += P::kRows;
     nz = reinterpret_cast<uint16_t*>(q);
     q += P::kNz;
+    vlist = reinterpret_cast<uint16_t*>(q);
+    q += P::kVList;
     misc = reinterpret_cast<int*>(q);
     q += P::kMisc;
     lists = reinterpret_cast<uint32_t*>(q);
@@ -268,8 +275,6 @@ struct ChunkSmem {
     colk = reinterpret_cast<int*>(q);
     ax = reinterpret_cast<AxisX*>(q + P::kColK);
     az = reinterpret_cast<AxisZ*>(q + P::kColK + P::kAxisHalf);
-    zmin = reinterpret_cast<int*>(q + P::kColK + P::kAxis);
-    zmax = zmin + N;
   }
 };
 
@@ -399,40 +404,77 @@ __device__ void gen_heightmap(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, 
     }
   }
   __syncthreads();
-  for (int z = t; z < N; z += T) {
-    int mn = N + 1, mx = -1;
-    for (int x = 0; x < N; ++x) {
-      const int k = s.colk[(z + 1) * side + x + 1];
-      mn = k < mn ? k : mn;
-      mx = k > mx ? k : mx;
-    }
-    s.zmin[z] = mn;
-    s.zmax[z] = mx;
-  }
-  __syncthreads();
-  for (int r = t; r < N * N; r += T) {
-    const int y = r / N, z = r % N;
-    RowT row = 0;
-    if (y < s.zmin[z]) {
-      row = full_row<N>();
-    } else if (y < s.zmax[z]) {
-      const int* kz = s.colk + (z + 1) * side + 1;
-      for (int x = 0; x < N; ++x) row |= (RowT)(y < kz[x] ? 1u : 0u) << x;
-    }
-    s.occ[r] = row;
-  }
-  if (with_halo) {
-    for (int i = t; i < 6 * N; i += T) {
-      const int h = i / N, a = i % N;
-      RowT row = 0;
-      if ((halo_mask >> h) & 1u) {
-        for (int b = 0; b < N; ++b) {
-          int x, y, z;
-          halo_coord<N>(h, a, b, x, y, z);
-          row |= (RowT)(y < s.colk[(z + 1) * side + x + 1] ? 1u : 0u) << b;
+  // Rows from the column thresholds, one warp task per group of columns: the own rows of
+  // a group of z values (and their -y / +y halo rows), or one lateral halo strip. Lanes
+  // hold one column's threshold k each; rows below the group's smallest k are full, rows
+  // at or above its largest k are empty, and the rows in between are ballots of y < k.
+  {
+    constexpr int G = N >= 32 ? 1 : 32 / N;  // z values per own-row task
+    constexpr int S = N > 32 ? N / 32 : 1;   // 32-bit words per row
+    constexpr int LW = N >= 32 ? 32 : N;     // lanes per row word
+    constexpr int W = Shape<N>::W;
+    constexpr uint32_t kWordFull = N >= 32 ? 0xFFFFFFFFu : ((1u << (N & 31)) - 1u);
+    constexpr int kOwnTasks = (N / G) * S;
+    const int lane = t & 31, warp = t >> 5;
+    constexpr int nwarps = T / 32;
+    uint32_t* occw = reinterpret_cast<uint32_t*>(s.occ);
+    uint32_t* halow = reinterpret_cast<uint32_t*>(s.halo);
+    const int sub = lane / LW, b = lane % LW;  // row word group and bit of this lane
+    for (int task = warp; task < kOwnTasks + 4 * S; task += nwarps) {
+      const bool own = task < kOwnTasks;
+      const int h = own ? -1 : (task - kOwnTasks) / S;
+      const int seg = own ? task % S : (task - kOwnTasks) % S;
+      const int xb = seg * 32 + b;  // bit position within the row
+      int k;
+      bool active = true;  // lanes past the end of a short halo strip hold no column
+      uint32_t* base;      // word of row a of the task's first row group: base[a * rstride]
+      int rstride;
+      if (own) {
+        const int z = (task / S) * G + sub;
+        k = s.colk[(z + 1) * side + xb + 1];
+        base = occw + (task / S) * G * W + seg;
+        rstride = N * W;
+      } else {
+        // lateral halo h: row a = y, bit = position along the strip
+        const int c = sub == 0 ? xb : -1;
+        active = c >= 0;
+        if (c < 0) k = -1;
+        else if (h == 0) k = s.colk[(c + 1) * side];
+        else if (h == 1) k = s.colk[(c + 1) * side + N + 1];
+        else if (h == 2) k = s.colk[c + 1];
+        else k = s.colk[(N + 1) * side + c + 1];
+        if (!((halo_mask >> h) & 1u) || !with_halo) k = -1;
+        base = halow + h * N * W + seg;
+        rstride = W;
+      }
+      const int kmin = __reduce_min_sync(0xffffffffu, active ? k : N + 1);
+      const int kmax = __reduce_max_sync(0xffffffffu, active ? k : -1);
+      // trivial rows (own tasks: G rows of each y; halo tasks: one row of each y)
+      const int gw = own ? G : 1;
+      for (int j = lane; j < N * gw; j += 32) {
+        const int y = j / gw, zz = j % gw;
+        base[y * rstride + zz * W] = y < kmin ? kWordFull : 0u;
+      }
+      __syncwarp();
+      const int y0 = kmin < 0 ? 0 : kmin, y1 = kmax > N ? N : kmax;
+      for (int y = y0; y < y1; ++y) {
+        const uint32_t bal = __ballot_sync(0xffffffffu, y < k);
+        if (b == 0 && (own || sub == 0))
+          base[y * rstride + sub * W] = N >= 32 ? bal : ((bal >> lane) & kWordFull);
+      }
+      if (own) {
+        // -y and +y halo rows of these z values (bits x): y = -1 and y = N
+        const bool use4 = with_halo && ((halo_mask >> 4) & 1u);
+        const bool use5 = with_halo && ((halo_mask >> 5) & 1u);
+        const uint32_t b4 = __ballot_sync(0xffffffffu, use4 && -1 < k);
+        const uint32_t b5 = __ballot_sync(0xffffffffu, use5 && N < k);
+        if (b == 0 && with_halo) {
+          const int z = (task / S) * G + sub;
+          halow[(4 * N + z) * W + seg] = N >= 32 ? b4 : ((b4 >> lane) & kWordFull);
+          halow[(5 * N + z) * W + seg] = N >= 32 ? b5 : ((b5 >> lane) & kWordFull);
         }
       }
-      s.halo[i] = row;
+      __syncwarp();
     }
   }
   __syncthreads();
@@ -560,16 +602,19 @@ __device__ __forceinline__ void row_masks(const ChunkSmem<N, LAYOUT>& s, int y, 
   m[5] = row & ~un;
 }
 
-// Per-row face counts -> exclusive offsets in s.rows[0..R] and the ascending list of the
-// rows with faces in s.nz (count in s.misc[0]); returns the chunk's face total.
+// Per-row face counts -> exclusive offsets in s.rows[0..R], the ascending list of the
+// rows with faces in s.nz (count in s.misc[0]) and, when they fit, the face voxels in
+// emission order in s.vlist (count in s.misc[1], else -1); returns the chunk's face total.
 template <int N, int LAYOUT, int T>
 __device__ uint32_t count_and_scan(ChunkSmem<N, LAYOUT>& s) {
   using RowT = typename Shape<N>::RowT;
   constexpr int RPT = Shape<N>::R / T;
+  constexpr int VCap = Shape<N>::VCap;
   static_assert(RPT >= 1 && RPT * T == Shape<N>::R, "rows must split evenly over threads");
   const int t = threadIdx.x;
   uint32_t cnt[RPT];
-  uint32_t local = 0, nzl = 0;
+  RowT any[RPT];
+  uint32_t local = 0, vl = 0, nzl = 0;
 #pragma unroll
   for (int k = 0; k < RPT; ++k) {
     const int r = t * RPT + k;
@@ -579,13 +624,17 @@ __device__ uint32_t count_and_scan(ChunkSmem<N, LAYOUT>& s) {
 #pragma unroll
     for (int d = 0; d < 6; ++d) c += (uint32_t)popc_row(m[d]);
     cnt[k] = c;
+    any[k] = VCap > 0 ? (m[0] | m[1] | m[2] | m[3] | m[4] | m[5]) : (RowT)0;
     local += c;
+    if (VCap > 0) vl += (uint32_t)popc_row(any[k]);
     nzl += c != 0u ? 1u : 0u;
   }
-  // Deterministic block scan of (faces << 16 | rows with faces): warp inclusive scan,
-  // then a scan of the warp totals.
+  // Deterministic block scan of (faces << 40 | face voxels << 20 | rows with faces); each
+  // field stays below 2^20 (at most 3N^3 + 6N^2 faces): warp inclusive scan, then a scan
+  // of the warp totals.
   const int lane = t & 31, warp = t >> 5, nwarps = T >> 5;
-  const unsigned long long mine = ((unsigned long long)local << 16) | nzl;
+  const unsigned long long mine =
+      ((unsigned long long)local << 40) | ((unsigned long long)vl << 20) | nzl;
   unsigned long long incl = mine;
 #pragma unroll
   for (int off = 1; off < 32; off <<= 1) {
@@ -608,20 +657,32 @@ __device__ uint32_t count_and_scan(ChunkSmem<N, LAYOUT>& s) {
   }
   __syncthreads();
   const unsigned long long excl = wsum[32 + warp] + incl - mine;
-  uint32_t run = (uint32_t)(excl >> 16);
-  uint32_t nzrun = (uint32_t)(excl & 0xFFFFu);
+  const unsigned long long tot = wsum[64];
+  const uint32_t nvox = (uint32_t)(tot >> 20) & 0xFFFFFu;
+  const bool use_list = VCap > 0 && nvox <= (uint32_t)VCap;
+  uint32_t run = (uint32_t)(excl >> 40);
+  uint32_t vrun = (uint32_t)(excl >> 20) & 0xFFFFFu;
+  uint32_t nzrun = (uint32_t)excl & 0xFFFFFu;
 #pragma unroll
   for (int k = 0; k < RPT; ++k) {
     const int r = t * RPT + k;
     s.rows[r] = run;
     if (cnt[k] != 0u) s.nz[nzrun++] = (uint16_t)r;
+    if (VCap > 0 && use_list) {
+      RowT u = any[k];
+      while (u) {
+        const int x = __ffs((uint32_t)u) - 1;
+        u &= u - (RowT)1;
+        s.vlist[vrun++] = (uint16_t)((r << Shape<N>::LOG2N) | x);
+      }
+    }
     run += cnt[k];
   }
-  const unsigned long long tot = wsum[64];
-  const uint32_t total = (uint32_t)(tot >> 16);
+  const uint32_t total = (uint32_t)(tot >> 40);
   if (t == 0) {
     s.rows[Shape<N>::R] = total;
-    s.misc[0] = (int)(tot & 0xFFFFu);
+    s.misc[0] = (int)(tot & 0xFFFFFu);
+    s.misc[1] = use_list ? (int)nvox : -1;
   }
   __syncthreads();
   return total;
@@ -799,14 +860,15 @@ __device__ __forceinline__ uint32_t pack_face(int x, int y, int z, int d) {
   return (uint32_t)x | ((uint32_t)y << 7) | ((uint32_t)z << 14) | ((uint32_t)d << 21);
 }
 
-// Face compaction of one warp: lane l owns element base + l of the window's rows with
-// faces (rows nz[k0..], N voxels each, so the warp's voxels are consecutive in emission
-// order). Each lane lists its voxel's faces in direction order into the warp's face list;
-// returns the warp's face count and, in `first`, the window-relative index of the warp's
-// first face (face i of the list has index first + i).
+// Face compaction of one warp: lane l owns element base + l of the chunk's emission
+// elements, the face voxels of s.vlist (use_list) or else every voxel of the rows with
+// faces (rows nz[], N voxels each); either way the warp's voxels are consecutive in
+// emission order. Each lane lists its voxel's faces in direction order into the warp's
+// face list; returns the warp's face count and, in `first`, the chunk-relative index of
+// the warp's first face (face i of the list has index first + i).
 template <int N, int LAYOUT>
-__device__ __forceinline__ int warp_faces(const ChunkSmem<N, LAYOUT>& s, int k0, int elems,
-                                          int base, uint32_t f0, uint32_t* list, uint32_t& first) {
+__device__ __forceinline__ int warp_faces(const ChunkSmem<N, LAYOUT>& s, bool use_list,
+                                          int elems, int base, uint32_t* list, uint32_t& first) {
   using RowT = typename Shape<N>::RowT;
   const int lane = threadIdx.x & 31;
   const int e = base + lane;
@@ -814,23 +876,31 @@ __device__ __forceinline__ int warp_faces(const ChunkSmem<N, LAYOUT>& s, int k0,
   uint32_t mine = 0;
   int x = 0, y = 0, z = 0;
   if (e < elems) {
-    const int r = s.nz[k0 + e / N];
-    x = e % N;
+    int r;
+    if (Shape<N>::VCap > 0 && use_list) {
+      const uint32_t q = s.vlist[e];
+      x = (int)(q & (uint32_t)(N - 1));
+      r = (int)(q >> Shape<N>::LOG2N);
+    } else {
+      r = s.nz[e / N];
+      x = e % N;
+    }
     y = r / N;
     z = r % N;
     RowT m[6];
     row_masks<N, LAYOUT>(s, y, z, m);
 #pragma unroll
     for (int d = 0; d < 6; ++d) bits |= (unsigned)((m[d] >> x) & (RowT)1) << d;
-    // Only lane 0's position is needed (the warp scan places the others). A warp starts
+    // Only lane 0's position is needed (the warp scan places the others): the row's face
+    // offset plus the faces of the voxels before x in the row. Row by row, a warp starts
     // on a row boundary (x = 0) unless rows are 64 wide (x = 0 or 32).
     uint32_t pre = 0;
-    if (N > 32 && lane == 0 && x != 0) {
+    if ((use_list || N > 32) && lane == 0 && x != 0) {
       const RowT below = (RowT)(~(RowT)0) >> (sizeof(RowT) * 8 - x);
 #pragma unroll
       for (int d = 0; d < 6; ++d) pre += (uint32_t)popc_row(m[d] & below);
     }
-    mine = s.rows[r] - f0 + pre;
+    mine = s.rows[r] + pre;
   }
   const int cnt = __popc(bits);
   int incl = cnt;
@@ -854,24 +924,26 @@ __device__ __forceinline__ int warp_faces(const ChunkSmem<N, LAYOUT>& s, int k0,
 // Emits the faces of the chunk in reference order: chunk-local face f goes to global
 // face g0 + f. Every warp compacts the faces of its 32 voxels, stages them 32 at a time
 // in one of its two shared-memory buffers (one face record per lane, final byte layout)
-// and sends each batch to global memory with a TMA bulk copy issued by its lane 0. No
-// CTA-wide barrier: a warp waits only until the bulk copy that last read a buffer is
-// done before refilling it, and until all its copies have read shared memory at the end
-// (the staging area is reused by the next chunk's generation).
+// and sends each batch to global memory with a TMA bulk copy issued by its lane 0. A
+// warp has nbuf (1 or 2) such buffers. No CTA-wide barrier: a warp waits only until the
+// bulk copy that last read a buffer is done before refilling it, and until all its
+// copies have read shared memory at the end (the staging area is reused by the next
+// chunk's generation).
 template <int N, int LAYOUT>
 __device__ void emit_chunk(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c, unsigned long long g0,
-                           unsigned long long cap, void* out0, void* out1) {
+                           unsigned long long cap, void* out0, void* out1, int nbuf) {
   constexpr int kBuf = warp_buf_bytes<LAYOUT>();
-  const int nzc = s.misc[0];
+  const int nl = s.misc[1];
+  const bool use_list = nl >= 0;
+  const int elems = use_list ? nl : s.misc[0] * N;
   const int ox = c.x * N, oy = c.y * N, oz = c.z * N;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   uint32_t* list = s.lists + warp * kWarpFaces;
-  unsigned char* bufs = s.stage + (size_t)warp * 2 * kBuf;
+  unsigned char* bufs = s.stage + (size_t)warp * nbuf * kBuf;
   int b = 0;
-  const int elems = nzc * N;
   for (int base = warp * 32; base < elems; base += nwarps * 32) {
     uint32_t first;
-    const int nwf = warp_faces<N, LAYOUT>(s, 0, elems, base, 0u, list, first);
+    const int nwf = warp_faces<N, LAYOUT>(s, use_list, elems, base, list, first);
     for (int r0 = 0; r0 < nwf; r0 += kWarpBatch) {
       const int cnt = nwf - r0 < kWarpBatch ? nwf - r0 : kWarpBatch;
       const unsigned long long g = g0 + first + (unsigned)r0;
@@ -880,8 +952,11 @@ __device__ void emit_chunk(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c, unsigned 
       else if (g + (unsigned long long)cnt > cap) nw = (int)(cap - g);
       if (nw == 0) continue;
       unsigned char* buf = bufs + b * kBuf;
-      // the copy issued two batches ago read this buffer; wait until it is done reading
-      if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+      // the copy issued nbuf batches ago read this buffer; wait until it is done reading
+      if (lane == 0) {
+        if (nbuf == 1) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        else asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+      }
       __syncwarp();
       const int shift = stage_shift<LAYOUT>(g);
       if (lane < nw) {
@@ -894,7 +969,7 @@ __device__ void emit_chunk(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c, unsigned 
       __syncwarp();
       flush_warp<LAYOUT>(buf, shift, nw, g, out0, out1);
       __syncwarp();
-      b ^= 1;
+      b = nbuf == 2 ? b ^ 1 : 0;
     }
   }
   if (lane == 0) bulk_wait_read_all();
@@ -947,14 +1022,15 @@ template <int N, int LAYOUT>
 __device__ void emit_chunk_direct(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c,
                                   unsigned long long g0, unsigned long long cap, void* out0,
                                   void* out1) {
-  const int nzc = s.misc[0];
+  const int nl = s.misc[1];
+  const bool use_list = nl >= 0;
+  const int elems = use_list ? nl : s.misc[0] * N;
   const int ox = c.x * N, oy = c.y * N, oz = c.z * N;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   uint32_t* list = s.lists + warp * kWarpFaces;
-  const int elems = nzc * N;
   for (int base = warp * 32; base < elems; base += nwarps * 32) {
     uint32_t first;
-    const int nwf = warp_faces<N, LAYOUT>(s, 0, elems, base, 0u, list, first);
+    const int nwf = warp_faces<N, LAYOUT>(s, use_list, elems, base, list, first);
     for (int i = lane; i < nwf; i += 32) {
       const uint32_t q = list[i];
       const int x = q & 127, y = (q >> 7) & 127, z = (q >> 14) & 127, d = q >> 21;
@@ -974,6 +1050,39 @@ __device__ void emit_chunk_direct(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c,
 
 // Persistent fused generation + meshing over a device work queue (GM != GM_OCC), or
 // meshing of resident occupancy (GM == GM_OCC). One chunk per CTA iteration; T threads.
+// Occupancy and halo rows of chunk i in shared memory: loaded from the slot pool
+// (GM_OCC) or generated from the noise field.
+template <int N, int GM, int LAYOUT, int T>
+__device__ __forceinline__ void prepare_chunk(ChunkSmem<N, LAYOUT>& s, const MeshArgs& a, int i,
+                                              vox_chunk_coord c) {
+  if (GM == GM_OCC) {
+    const unsigned long long words = (unsigned long long)N * N * Shape<N>::W;
+    const int slot = a.slots[i];
+    const uint32_t* nb[6];
+    unsigned use = 0;
+    bool bad = slot < 0 || slot >= a.pool_slots;
+    for (int d = 0; d < 6; ++d) {
+      const int ns = a.nbr_slots ? a.nbr_slots[6 * i + d] : -1;
+      nb[d] = nullptr;
+      if (d >= 4 && !a.full6) continue;
+      if (ns >= a.pool_slots) bad = true;
+      if (ns >= 0 && ns < a.pool_slots) {
+        nb[d] = a.occ_pool + (unsigned long long)ns * words;
+        use |= 1u << d;
+      }
+    }
+    if (bad && threadIdx.x == 0) atomicOr(&a.ctl->err, ERR_BAD_INPUT);
+    // An out-of-range slot reads slot 0 instead (the call then reports VOX_ERR_INVALID).
+    const int sl = (slot >= 0 && slot < a.pool_slots) ? slot : 0;
+    load_chunk<N, LAYOUT>(s, a.occ_pool + (unsigned long long)sl * words, nb, use);
+  } else {
+    unsigned m = a.nbr_mask ? a.nbr_mask[i] : 0u;
+    if (GM == GM_BERNOULLI) m = 0u;
+    if (!a.full6) m &= 0xFu;
+    gen_chunk<N, GM, LAYOUT, T>(s, a.gen, c, a.index_base + i, m, true);
+  }
+}
+
 template <int N, int GM, int LAYOUT, int T>
 __global__ void __launch_bounds__(T)
 k_mesh_batch(MeshArgs a) {
@@ -987,14 +1096,12 @@ k_mesh_batch(MeshArgs a) {
   if (threadIdx.x == 0) {
     s_epoch = ld_relaxed_u32(&a.ctl->epoch);
     __threadfence();
+    s_item = (int)atomicAdd(&a.ctl->next, 1u);
   }
   __syncthreads();
   const unsigned epoch = s_epoch;
-  const unsigned long long words = (unsigned long long)N * N * Shape<N>::W;
+  int i = s_item;
   while (true) {
-    if (threadIdx.x == 0) s_item = (int)atomicAdd(&a.ctl->next, 1u);
-    __syncthreads();
-    const int i = s_item;
     if (i >= a.n) {
       if (threadIdx.x == 0 && i == a.n + (int)gridDim.x - 1) {
         // The last ticket of this launch: reset the queue and advance the epoch.
@@ -1003,32 +1110,13 @@ k_mesh_batch(MeshArgs a) {
       }
       break;
     }
+    // The next ticket is drawn now and used after this chunk, so the atomic's latency
+    // overlaps the chunk's work. A CTA reserves chunks in increasing order, so the
+    // lowest unfinished chunk is always being processed and every look-back ends.
+    int next_item = 0;
+    if (threadIdx.x == 0) next_item = (int)atomicAdd(&a.ctl->next, 1u);
     const vox_chunk_coord c = a.coords[i];
-    if (GM == GM_OCC) {
-      const int slot = a.slots[i];
-      const uint32_t* nb[6];
-      unsigned use = 0;
-      bool bad = slot < 0 || slot >= a.pool_slots;
-      for (int d = 0; d < 6; ++d) {
-        const int ns = a.nbr_slots ? a.nbr_slots[6 * i + d] : -1;
-        nb[d] = nullptr;
-        if (d >= 4 && !a.full6) continue;
-        if (ns >= a.pool_slots) bad = true;
-        if (ns >= 0 && ns < a.pool_slots) {
-          nb[d] = a.occ_pool + (unsigned long long)ns * words;
-          use |= 1u << d;
-        }
-      }
-      if (bad && threadIdx.x == 0) atomicOr(&a.ctl->err, ERR_BAD_INPUT);
-      // An out-of-range slot reads slot 0 instead (the call then reports VOX_ERR_INVALID).
-      const int sl = (slot >= 0 && slot < a.pool_slots) ? slot : 0;
-      load_chunk<N, LAYOUT>(s, a.occ_pool + (unsigned long long)sl * words, nb, use);
-    } else {
-      unsigned m = a.nbr_mask ? a.nbr_mask[i] : 0u;
-      if (GM == GM_BERNOULLI) m = 0u;
-      if (!a.full6) m &= 0xFu;
-      gen_chunk<N, GM, LAYOUT, T>(s, a.gen, c, a.index_base + i, m, true);
-    }
+    prepare_chunk<N, GM, LAYOUT, T>(s, a, i, c);
     const uint32_t total = count_and_scan<N, LAYOUT, T>(s);
     if (threadIdx.x < 32) {
       const unsigned long long excl =
@@ -1043,9 +1131,210 @@ k_mesh_batch(MeshArgs a) {
       }
     }
     __syncthreads();
-    if (a.stage_faces > 0) emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1);
+    if (a.stage_faces > 0)
+      emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch);
     else emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1);
+    if (threadIdx.x == 0) s_item = next_item;
     __syncthreads();
+    i = s_item;
+  }
+  if ((threadIdx.x & 31) == 0) bulk_wait_all();  // every lane 0 issued bulk copies
+}
+
+// ------------------------------------------------------------------------------------
+// Phased schedule of the fused batch kernel (cooperative launch: the whole grid is
+// resident, so CTAs may wait for one another).
+//  A. CTAs take chunks from the work queue, prepare and count them, and spill the
+//     occupancy + halo rows to a per-chunk scratch (L2-resident) and the face total to
+//     counts[i].
+//  B. Grid barrier. CTA 0 scans counts[] into face_offsets[] and raises the scan flag.
+//  C. CTAs take chunks from the second queue, reload and recount them (row offsets),
+//     wait for the scan flag once, and emit at face_offsets[i].
+// There is no chunk-to-chunk dependency inside a phase. The output bytes are the same
+// as the look-back schedule's.
+// ------------------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid barrier, called by thread 0 of every CTA after a __syncthreads. The last CTA to
+// arrive resets the arrival count and the first work queue, then advances the
+// generation; the others poll the generation at most spin_limit times. Returns the new
+// generation, or 0xFFFFFFFF after a timeout (ERR_TIMEOUT is set).
+static __device__ unsigned grid_barrier_t0(BatchCtl* ctl, unsigned nblocks, int spin_limit) {
+  const unsigned gen = ld_acquire_u32(&ctl->bar_gen);
+  __threadfence();  // this CTA's earlier writes are visible before its arrival
+  const unsigned arrived = atomicAdd(&ctl->bar_count, 1u);
+  if (arrived == nblocks - 1u) {
+    ctl->bar_count = 0u;
+    ctl->next = 0u;
+    __threadfence();
+    st_release_u32(&ctl->bar_gen, gen + 1u);
+    return gen + 1u;
+  }
+  int spins = 0;
+  while (ld_acquire_u32(&ctl->bar_gen) == gen) {
+    if (++spins > spin_limit) {
+      atomicOr(&ctl->err, ERR_TIMEOUT);
+      return 0xFFFFFFFFu;
+    }
+    __nanosleep(spins < 8 ? 32 : 256);
+  }
+  __threadfence();
+  return gen + 1u;
+}
+
+// Deterministic exclusive scan of counts[0, n) into offs[0, n), total at offs[n]
+// (one CTA of T threads, 8 counts per thread per tile). Returns the total.
+template <int T>
+__device__ unsigned long long scan_counts(const uint32_t* counts, int n,
+                                          unsigned long long* offs, unsigned long long* wsum) {
+  constexpr int V = 8;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarps = T >> 5;
+  unsigned long long carry = 0;
+  for (int base = 0; base < n; base += T * V) {
+    uint32_t v[V];
+    unsigned long long local = 0;
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const int idx = base + t * V + k;
+      v[k] = idx < n ? __ldcg(counts + idx) : 0u;
+      local += v[k];
+    }
+    unsigned long long incl = local;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+      const unsigned long long u = __shfl_up_sync(0xffffffffu, incl, off);
+      if (lane >= off) incl += u;
+    }
+    if (lane == 31) wsum[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+      const unsigned long long w = lane < nwarps ? wsum[lane] : 0ull;
+      unsigned long long wi = w;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const unsigned long long u = __shfl_up_sync(0xffffffffu, wi, off);
+        if (lane >= off) wi += u;
+      }
+      if (lane < nwarps) wsum[32 + lane] = wi - w;
+      if (lane == nwarps - 1) wsum[64] = wi;
+    }
+    __syncthreads();
+    unsigned long long run = carry + wsum[32 + warp] + incl - local;
+#pragma unroll
+    for (int k = 0; k < V; ++k) {
+      const int idx = base + t * V + k;
+      if (idx < n) offs[idx] = run;
+      run += v[k];
+    }
+    carry += wsum[64];
+    __syncthreads();  // wsum is reused by the next tile
+  }
+  if (t == 0) offs[n] = carry;
+  return carry;
+}
+
+template <int N, int GM, int LAYOUT, int T>
+__global__ void __launch_bounds__(T)
+k_mesh_batch_phased(MeshArgs a) {
+  using P = SmemPlan<N, LAYOUT>;
+  constexpr int kSpill16 = (P::kOcc + P::kHalo) / 16;  // occupancy + halo rows, in uint4
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  ChunkSmem<N, LAYOUT> s;
+  s.carve(smem_raw);
+  load_tables<N, LAYOUT>(s, a.tables);
+  __shared__ int s_item;
+  __shared__ unsigned s_gen;
+  __shared__ unsigned long long s_base;
+  uint4* const spill = reinterpret_cast<uint4*>(a.scratch);
+  uint4* const occ16 = reinterpret_cast<uint4*>(s.occ);  // s.halo follows s.occ
+  __syncthreads();
+
+  // A. prepare + count + spill (the next ticket is drawn before the chunk's work)
+  if (threadIdx.x == 0) s_item = (int)atomicAdd(&a.ctl->next, 1u);
+  __syncthreads();
+  for (int i = s_item; i < a.n;) {
+    int next_item = 0;
+    if (threadIdx.x == 0) next_item = (int)atomicAdd(&a.ctl->next, 1u);
+    prepare_chunk<N, GM, LAYOUT, T>(s, a, i, a.coords[i]);
+    const uint32_t total = count_and_scan<N, LAYOUT, T>(s);
+    uint4* dst = spill + (unsigned long long)i * kSpill16;
+    for (int k = threadIdx.x; k < kSpill16; k += T) __stcg(dst + k, occ16[k]);
+    if (threadIdx.x == 0) {
+      __stcg(a.counts + i, total);
+      s_item = next_item;
+    }
+    __syncthreads();
+    i = s_item;
+  }
+
+  // B. barrier; CTA 0 scans the counts
+  __syncthreads();
+  if (threadIdx.x == 0) s_gen = grid_barrier_t0(a.ctl, gridDim.x, a.spin_limit);
+  __syncthreads();
+  const unsigned gen = s_gen;
+  if (gen == 0xFFFFFFFFu) return;
+  if (blockIdx.x == 0) {
+    const unsigned long long total = scan_counts<T>(a.counts, a.n, a.face_offsets,
+                                                    reinterpret_cast<unsigned long long*>(s.stage));
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      if (total > a.cap) atomicOr(&a.ctl->err, ERR_CAPACITY);
+      __threadfence();
+      st_release_u32(&a.ctl->scan_flag, gen);
+    }
+  }
+
+  // C. reload + recount + emit
+  bool scanned = blockIdx.x == 0;  // thread 0's view: the scan flag has been seen
+  if (threadIdx.x == 0) s_item = (int)atomicAdd(&a.ctl->next2, 1u);
+  __syncthreads();
+  int i = s_item;
+  while (true) {
+    if (i >= a.n) {
+      // The last ticket of this launch resets the second queue.
+      if (threadIdx.x == 0 && i == a.n + (int)gridDim.x - 1) a.ctl->next2 = 0u;
+      break;
+    }
+    int next_item = 0;
+    if (threadIdx.x == 0) next_item = (int)atomicAdd(&a.ctl->next2, 1u);
+    const vox_chunk_coord c = a.coords[i];
+    const uint4* src = spill + (unsigned long long)i * kSpill16;
+    for (int k = threadIdx.x; k < kSpill16; k += T) occ16[k] = __ldcg(src + k);
+    __syncthreads();
+    count_and_scan<N, LAYOUT, T>(s);
+    if (threadIdx.x == 0) {
+      int spins = 0;
+      while (!scanned) {
+        if (ld_acquire_u32(&a.ctl->scan_flag) == gen) {
+          scanned = true;
+          break;
+        }
+        if (++spins > a.spin_limit) break;
+        __nanosleep(spins < 8 ? 32 : 256);
+      }
+      if (scanned) {
+        s_base = __ldcg(a.face_offsets + i);
+      } else {
+        atomicOr(&a.ctl->err, ERR_TIMEOUT);
+        s_base = ~0ull;
+      }
+    }
+    __syncthreads();
+    if (s_base == ~0ull) break;  // the scan flag never came: give up (error reported)
+    if (a.stage_faces > 0)
+      emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch);
+    else emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1);
+    if (threadIdx.x == 0) s_item = next_item;
+    __syncthreads();
+    i = s_item;
   }
   if ((threadIdx.x & 31) == 0) bulk_wait_all();  // every lane 0 issued bulk copies
 }
@@ -1067,7 +1356,8 @@ k_mesh_single(MeshArgs a) {
     a.face_offsets[0] = total;
     if ((unsigned long long)total > a.cap) atomicOr(&a.ctl->err, ERR_CAPACITY);
   }
-  if (a.stage_faces > 0) emit_chunk<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.out0, a.out1);
+  if (a.stage_faces > 0)
+    emit_chunk<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch);
   else emit_chunk_direct<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.out0, a.out1);
   if ((threadIdx.x & 31) == 0) bulk_wait_all();
 }

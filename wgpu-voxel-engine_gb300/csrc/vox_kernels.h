@@ -9,9 +9,11 @@ struct KernelSet {
   int n_size;                   // chunk size N
   int threads[2];               // the two CTA sizes the meshing kernels exist in
   const void* batch[4][2][2];   // k_mesh_batch<N, gen mode, layout, threads[t]>
+  const void* phased[4][2][2];  // k_mesh_batch_phased<N, gen mode, layout, threads[t]>
   const void* single[2][2];     // k_mesh_single<N, layout, threads[t]>
   const void* generate[4];      // k_generate<N, gen mode, gen_threads> (index 0 unused)
   int gen_threads;
+  int spill_bytes;              // occupancy + halo rows of one chunk (phased scratch)
   // dynamic shared memory of a launch (layout, CTA size, staging window in faces)
   int (*smem_total)(int layout, int threads, int stage_faces);
 };

@@ -17,6 +17,7 @@
 // calls whose work overlaps on the GPU race on the shared array.
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -33,9 +34,11 @@ constexpr int kNoAllocMaxChunks = 16384;  // chunks per call
 
 struct NoAllocScratch {
   BatchCtl ctl;                                // queue ticket, epoch, error bits
-  unsigned long long pad[30];                  // keeps the states on a 256-byte boundary
+  unsigned char pad[256 - sizeof(BatchCtl)];   // keeps the states on a 256-byte boundary
   unsigned long long state[kNoAllocMaxChunks]; // look-back states
 };
+static_assert(sizeof(BatchCtl) <= 256 && offsetof(NoAllocScratch, state) == 256,
+              "look-back states start 256 bytes into the scratch");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
 

@@ -29,6 +29,7 @@ VOX_ERR_TIMEOUT, VOX_ERR_CAPACITY, VOX_ERR_NO_DEVICE = 4, 5, 6
 GEN_HEIGHTMAP, GEN_DENSITY, GEN_BERNOULLI = 0, 1, 2
 CULL_REFERENCE, CULL_FULL6 = 0, 1
 LAYOUT_VERTEX, LAYOUT_INSTANCED = 0, 1
+SCHEDULE_LOOKBACK, SCHEDULE_PHASED = 0, 1
 # TEXTURE_INDEX_LIST row of GRASS (src/texture.rs:240-243), by face slot L R Bk F Up Down.
 GRASS_TEXTURES = (0, 0, 0, 0, 2, 1)
 
@@ -63,11 +64,12 @@ class Sizes(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int32), ("stage_faces", ctypes.c_int32),
-                ("ctas_per_sm", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                ("ctas_per_sm", ctypes.c_int32), ("schedule", ctypes.c_int32)]
 
     def as_dict(self):
         return {"threads": self.threads, "stage_faces": self.stage_faces,
-                "ctas_per_sm": self.ctas_per_sm}
+                "ctas_per_sm": self.ctas_per_sm,
+                "schedule": "phased" if self.schedule == SCHEDULE_PHASED else "lookback"}
 
 
 class ServeConfig(ctypes.Structure):
@@ -310,8 +312,9 @@ class Context:
         self._check(self._lib.vox_ctx_get_tuning(self._h, ctypes.byref(t)), "vox_ctx_get_tuning")
         return t
 
-    def set_tuning(self, threads: int, stage_faces: int, ctas_per_sm: int = 0):
-        t = Tuning(threads, stage_faces, ctas_per_sm, 0)
+    def set_tuning(self, threads: int, stage_faces: int, ctas_per_sm: int = 0,
+                   schedule: int = 0):
+        t = Tuning(threads, stage_faces, ctas_per_sm, schedule)
         self._check(self._lib.vox_ctx_set_tuning(self._h, ctypes.byref(t)), "vox_ctx_set_tuning")
 
     def autotune(self, d_coords, d_nbr_mask, n: int, d_out0, d_out1, cap_faces: int, d_offsets,
