@@ -428,8 +428,9 @@ def plain_per_chunk(ctx, wl, cfg, d_coords, stream, args, b0, b1, torch, np):
 
 
 def e2e_host(ctx, wl, masks, n, total_faces, b0, b1, args, np):
-    """vox_gen_mesh_host with pinned host buffers: H2D of coordinates and neighbour masks,
-    the fused launch, D2H of offsets and every emitted face, all inside the timed call."""
+    """vox_gen_mesh_host with pinned host buffers: the coordinates and neighbour masks
+    come from host memory and every emitted face and offset lands in host memory, all
+    inside the timed call (the kernel reads and writes the page-locked buffers in place)."""
     import ctypes
 
     import voxgpu
@@ -462,7 +463,8 @@ def e2e_host(ctx, wl, masks, n, total_faces, b0, b1, args, np):
     ms = 1e3 * statistics.median(times)
     return {"value": n / (ms / 1e3), "unit": "chunks/s", "ms_per_step": ms,
             "h2d_bytes_per_step": n * 13, "d2h_bytes_per_step": (n + 1) * 8 + total_faces * (b0 + b1),
-            "api": "vox_gen_mesh_host (pinned host buffers, synchronous)"}
+            "api": "vox_gen_mesh_host (pinned host buffers: the kernel reads the inputs and "
+                   "writes faces and offsets in host memory over NVLink-C2C; synchronous)"}
 
 
 def serving_run(frames: int, paced: bool, view_radius: int = 24, slots: int = 4,

@@ -212,8 +212,11 @@ int vox_gen_mesh_batch_noalloc(const vox_config* cfg, void* stream,
                                int32_t n, int64_t chunk_index_base, void* d_out0, void* d_out1,
                                uint64_t cap_faces, uint64_t* d_face_offsets);
 
-/* Same as vox_gen_mesh_batch with host buffers: copies the inputs in, runs the fused
- * kernel, and copies exactly the emitted faces and the offsets back. Synchronous. */
+/* Same as vox_gen_mesh_batch with host buffers. Synchronous. When h_out0 (h_out1) and
+ * h_face_offsets are page-locked (vox_host_alloc, cudaMallocHost, cudaHostRegister) and
+ * 16-byte aligned, the kernel writes the faces and offsets straight into them (over
+ * NVLink-C2C on Grace systems) and page-locked inputs are read in place; otherwise the
+ * inputs are copied in and exactly the emitted faces and the offsets are copied back. */
 int vox_gen_mesh_host(vox_ctx* ctx, const vox_chunk_coord* h_coords, const uint8_t* h_nbr_mask,
                       int32_t n, int64_t chunk_index_base, void* h_out0, void* h_out1,
                       uint64_t cap_faces, uint64_t* h_face_offsets);

@@ -83,3 +83,24 @@ def gpu_generate(vox, cfg, coords, index_base=0):
     out = to_np(occ, n * words * 4).view(np.uint32).reshape(n, words)
     ctx.close()
     return out
+
+
+class Pinned:
+    """A page-locked host buffer from vox_host_alloc with a numpy view."""
+
+    def __init__(self, vox, nbytes):
+        import ctypes
+        self._lib = vox.lib()
+        p = ctypes.c_void_p()
+        assert self._lib.vox_host_alloc(max(16, int(nbytes)), ctypes.byref(p)) == 0
+        self.ptr = p.value
+        self.nbytes = int(nbytes)
+        self.a = np.ctypeslib.as_array((ctypes.c_uint8 * max(16, int(nbytes))).from_address(self.ptr))
+
+    def view(self, dtype):
+        return self.a[:self.nbytes].view(dtype)
+
+    def free(self):
+        if self.ptr:
+            self._lib.vox_host_free(self.ptr)
+            self.ptr = None

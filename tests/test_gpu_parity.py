@@ -6,7 +6,8 @@ instance records must equal the oracle's on the same inputs (signed zeros includ
 import numpy as np
 import pytest
 
-from gpu_util import ctx_for, dev_bytes, gpu_gen_mesh, gpu_generate, to_dev, to_np, use_schedule
+from gpu_util import (Pinned, ctx_for, dev_bytes, gpu_gen_mesh, gpu_generate, to_dev, to_np,
+                      use_schedule)
 
 pytestmark = pytest.mark.gpu
 
@@ -271,6 +272,44 @@ def test_repeat_launches_identical(vox):
         digests.append((total, hash(to_np(o0, total * 96).tobytes()),
                         hash(to_np(o1, total * 24).tobytes())))
     assert len(set(digests)) == 1
+    ctx.close()
+
+
+@pytest.mark.parametrize("schedule", SCHEDULES)
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_host_entry_point_pinned_zero_copy(vox, oracle, schedule, layout):
+    """Page-locked host buffers: the kernel writes faces and offsets in host memory."""
+    wl = vox.workload("heightmap")
+    cfg = wl.config(layout=layout)
+    n = 200
+    coords = np.asarray(wl.coords[:n], np.int32)
+    masks = np.asarray(vox.neighbour_masks(wl.coords[:n]), np.uint8)
+    w0, w1, woffs = oracle.gen_mesh_batch(cfg, wl.coords[:n], masks)
+    total = int(woffs[-1])
+    ctx = ctx_for(vox, cfg)
+    use_schedule(ctx, schedule)
+    b0, b1 = ctx.sizes.bytes_per_face_out0, ctx.sizes.bytes_per_face_out1
+    hc, hm = Pinned(vox, coords.nbytes), Pinned(vox, masks.nbytes)
+    hc.view(np.int32)[:] = coords.reshape(-1)
+    hm.view(np.uint8)[:] = masks
+    h0, h1, ho = Pinned(vox, total * b0), Pinned(vox, max(total * b1, 16)), Pinned(vox, (n + 1) * 8)
+    p1 = h1.ptr if b1 else None
+    for rep in range(2):
+        h0.a.fill(0xEE)
+        ctx.gen_mesh_host(hc.ptr, hm.ptr, n, h0.ptr, p1, total, ho.ptr)
+        assert np.array_equal(ho.view(np.uint64), woffs), rep
+        assert np.array_equal(h0.view(np.uint8), w0), rep
+        if b1:
+            assert np.array_equal(h1.view(np.uint8), w1), rep
+    # pageable inputs with page-locked outputs
+    ctx.gen_mesh_host(coords, masks, n, h0.ptr, p1, total, ho.ptr)
+    assert np.array_equal(h0.view(np.uint8), w0) and np.array_equal(ho.view(np.uint64), woffs)
+    st = ctx.gen_mesh_host(hc.ptr, hm.ptr, n, h0.ptr, p1, total - 1, ho.ptr,
+                           raise_on_error=False)
+    assert st == vox.VOX_ERR_CAPACITY and int(ho.view(np.uint64)[-1]) == total
+    assert np.array_equal(h0.view(np.uint8)[:(total - 1) * b0], w0[:(total - 1) * b0])
+    for b in (hc, hm, h0, h1, ho):
+        b.free()
     ctx.close()
 
 

@@ -45,6 +45,7 @@ struct vox_ctx {
   int spin_limit = kSpinLimit;
   int batch_grid[4] = {0, 0, 0, 0};   // persistent grid per gen mode (look-back kernel)
   int phased_grid[4] = {0, 0, 0, 0};  // co-resident grid per gen mode (phased kernel)
+  int host_grid[4] = {0, 0, 0, 0};    // grid of launches that write host memory (staged)
   // phased schedule: per-chunk occupancy + halo spill and face totals
   uint32_t* d_scratch = nullptr;
   uint32_t* d_counts = nullptr;
@@ -175,18 +176,23 @@ int apply_tuning(vox_ctx* ctx, int topt, int stage_faces, int ctas_per_sm, int s
   const int smem = ks.smem_total(layout, ks.threads[topt], stage_faces);
   if (smem > ctx->max_smem_optin - 256)
     return fail(ctx, VOX_ERR_INVALID, "staging window exceeds shared memory");
-  int grid[4], pgrid[4];
+  int grid[4], pgrid[4], hgrid[4];
+  const int hsmem = ks.smem_total(layout, ks.threads[topt], kStageSingle);
   for (int gm = 0; gm < 4; ++gm) {
-    for (int k = 0; k < 2; ++k) {
+    for (int k = 0; k < 3; ++k) {
       // the phased kernel's grid must be co-resident (cooperative launch): its occupancy
-      // is an upper bound, never exceeded
-      const void* fn = k == 0 ? ks.batch[gm][layout][topt] : ks.phased[gm][layout][topt];
+      // is an upper bound, never exceeded. k = 2: the selected schedule's kernel with one
+      // staging buffer per warp (launches whose outputs are in host memory)
+      const void* fn = k == 0 ? ks.batch[gm][layout][topt]
+                     : k == 1 ? ks.phased[gm][layout][topt]
+                     : (schedule == VOX_SCHEDULE_PHASED ? ks.phased : ks.batch)[gm][layout][topt];
       int per_sm = 0;
-      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, ks.threads[topt], smem);
+      cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, ks.threads[topt],
+                                                                    k == 2 ? hsmem : smem);
       if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
       if (per_sm < 1) return fail(ctx, VOX_ERR_INVALID, "kernel does not fit on an SM");
       if (ctas_per_sm > 0) per_sm = std::min(per_sm, ctas_per_sm);
-      (k == 0 ? grid : pgrid)[gm] = per_sm * ctx->num_sms;
+      (k == 0 ? grid : k == 1 ? pgrid : hgrid)[gm] = per_sm * ctx->num_sms;
     }
   }
   ctx->topt = topt;
@@ -196,6 +202,7 @@ int apply_tuning(vox_ctx* ctx, int topt, int stage_faces, int ctas_per_sm, int s
   for (int gm = 0; gm < 4; ++gm) {
     ctx->batch_grid[gm] = grid[gm];
     ctx->phased_grid[gm] = pgrid[gm];
+    ctx->host_grid[gm] = hgrid[gm];
   }
   return VOX_OK;
 }
@@ -277,10 +284,16 @@ int check_outputs(vox_ctx* ctx, void* out0, void* out1, uint64_t cap) {
   return VOX_OK;
 }
 
-int batch_launch(vox_ctx* ctx, MeshArgs& a, int gm) {
+// host_out: the outputs are in host memory; the launch stages every warp's faces in one
+// shared-memory buffer and writes them out with plain full-line stores.
+int batch_launch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out = false) {
   const int layout = ctx->cfg.layout;
   const int threads = ctx->ks->threads[ctx->topt];
-  const int smem = ctx->ks->smem_total(layout, threads, ctx->stage_faces);
+  const int smem = ctx->ks->smem_total(layout, threads, host_out ? kStageSingle : ctx->stage_faces);
+  if (host_out) {
+    a.stage_faces = kStageSingle;
+    a.lane_flush = 1;
+  }
   if (ctx->schedule == VOX_SCHEDULE_PHASED) {
     int st = ensure_scratch(ctx, (size_t)a.n);
     if (st != VOX_OK) return st;
@@ -288,7 +301,7 @@ int batch_launch(vox_ctx* ctx, MeshArgs& a, int gm) {
     a.counts = ctx->d_counts;
     ++ctx->launches;
     const void* fn = ctx->ks->phased[gm][layout][ctx->topt];
-    const int grid = std::max(1, std::min(a.n, ctx->phased_grid[gm]));
+    const int grid = std::max(1, std::min(a.n, host_out ? ctx->host_grid[gm] : ctx->phased_grid[gm]));
     void* params[] = {&a};
     VOX_CUDA(ctx, cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), params, (size_t)smem,
                                               ctx->stream),
@@ -301,7 +314,7 @@ int batch_launch(vox_ctx* ctx, MeshArgs& a, int gm) {
   if (st != VOX_OK) return st;
   a.state = ctx->d_state;
   const void* fn = ctx->ks->batch[gm][layout][ctx->topt];
-  const int grid = std::max(1, std::min(a.n, ctx->batch_grid[gm]));
+  const int grid = std::max(1, std::min(a.n, host_out ? ctx->host_grid[gm] : ctx->batch_grid[gm]));
   void* params[] = {&a};
   return launch(ctx, fn, grid, threads, smem, params);
 }
@@ -584,6 +597,18 @@ static int grow(vox_ctx* ctx, void** p, size_t* cap, size_t need, const char* wh
   return VOX_OK;
 }
 
+// Device address of page-locked host memory (cudaMallocHost / cudaHostRegister), or
+// nullptr for pageable memory.
+static void* mapped_host(const void* h) {
+  if (!h) return nullptr;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 int vox_gen_mesh_host(vox_ctx* ctx, const vox_chunk_coord* h_coords, const uint8_t* h_nbr_mask,
                       int32_t n, int64_t chunk_index_base, void* h_out0, void* h_out1,
                       uint64_t cap_faces, uint64_t* h_face_offsets) {
@@ -598,6 +623,46 @@ int vox_gen_mesh_host(vox_ctx* ctx, const vox_chunk_coord* h_coords, const uint8
   const size_t b0 = (size_t)bytes_out0(layout), b1 = (size_t)bytes_out1(layout);
   const size_t in_bytes = (size_t)n * sizeof(vox_chunk_coord) + (h_nbr_mask ? (size_t)n : 0);
   int st;
+  // Page-locked outputs: the kernel writes the faces and the offsets straight into host
+  // memory (over NVLink-C2C on Grace systems), staging each warp's faces in shared memory
+  // so that every store is a full-line write; one launch, one sync.
+  {
+    void* z0 = cap_faces > 0 ? mapped_host(h_out0) : nullptr;
+    void* z1 = cap_faces > 0 && b1 ? mapped_host(h_out1) : nullptr;
+    void* zoff = mapped_host(h_face_offsets);
+    const bool outs_ok = cap_faces == 0 || (z0 && aligned(z0, 16) && (b1 == 0 || (z1 && aligned(z1, 16))));
+    if (zoff && aligned(zoff, 8) && outs_ok) {
+      const void* zc = mapped_host(h_coords);
+      const void* zm = h_nbr_mask ? mapped_host(h_nbr_mask) : nullptr;
+      const vox_chunk_coord* d_coords = static_cast<const vox_chunk_coord*>(zc);
+      const uint8_t* d_mask = static_cast<const uint8_t*>(zm);
+      if (!zc || (h_nbr_mask && !zm)) {
+        if ((st = grow(ctx, &ctx->d_in, &ctx->in_cap, in_bytes, "cudaMalloc(inputs)")) != VOX_OK)
+          return st;
+        vox_chunk_coord* dc = static_cast<vox_chunk_coord*>(ctx->d_in);
+        uint8_t* dm = h_nbr_mask ? reinterpret_cast<uint8_t*>(dc + n) : nullptr;
+        VOX_CUDA(ctx, cudaMemcpyAsync(dc, h_coords, (size_t)n * sizeof(vox_chunk_coord),
+                                      cudaMemcpyHostToDevice, ctx->stream),
+                 "H2D coords");
+        if (h_nbr_mask)
+          VOX_CUDA(ctx, cudaMemcpyAsync(dm, h_nbr_mask, (size_t)n, cudaMemcpyHostToDevice, ctx->stream),
+                   "H2D mask");
+        d_coords = dc;
+        d_mask = dm;
+      }
+      MeshArgs a = base_args(ctx);
+      a.n = n;
+      a.index_base = chunk_index_base;
+      a.coords = d_coords;
+      a.nbr_mask = d_mask;
+      a.out0 = z0;
+      a.out1 = z1;
+      a.cap = cap_faces;
+      a.face_offsets = static_cast<unsigned long long*>(zoff);
+      if ((st = batch_launch(ctx, a, ctx->gm, true)) != VOX_OK) return st;
+      return sync_locked(ctx);  // the kernel flags a capacity overflow in the error word
+    }
+  }
   if ((st = grow(ctx, &ctx->d_in, &ctx->in_cap, in_bytes, "cudaMalloc(inputs)")) != VOX_OK) return st;
   size_t off_cap = ctx->offsets_cap * sizeof(unsigned long long);
   void* offp = ctx->d_offsets;

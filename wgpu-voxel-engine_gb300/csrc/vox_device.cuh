@@ -855,6 +855,46 @@ __device__ __forceinline__ void flush_warp(const unsigned char* buf, int shift, 
   }
 }
 
+// flush_warp with plain stores instead of bulk copies: the lanes copy the 16-byte aligned
+// part in 16-byte units (each warp store writes 512 contiguous bytes), then the head/tail
+// words. For outputs in host memory, where full-line writes matter most.
+template <int LAYOUT>
+__device__ __forceinline__ void flush_warp_lanes(const unsigned char* buf, int shift, int nw,
+                                                 unsigned long long g, void* out0, void* out1) {
+  const int lane = threadIdx.x & 31;
+  unsigned char* o0 = reinterpret_cast<unsigned char*>(out0);
+  if (LAYOUT == VOX_LAYOUT_INSTANCED) {
+    int l0 = (int)((4u - (unsigned)(g & 3ull)) & 3u);
+    if (l0 > nw) l0 = nw;
+    const int l1 = l0 + ((nw - l0) & ~3);
+    const unsigned char* src = buf + shift;
+    const uint4* s16 = reinterpret_cast<const uint4*>(src + (size_t)l0 * 68);
+    uint4* d16 = reinterpret_cast<uint4*>(o0 + (g + l0) * 68ull);
+    for (int q = lane; q < (l1 - l0) * 68 / 16; q += 32) d16[q] = s16[q];
+    const int head = l0 * 17, tail = (nw - l1) * 17;
+    for (int q = lane; q < head + tail; q += 32) {
+      const int w = q < head ? q : (l1 * 17 + (q - head));
+      reinterpret_cast<uint32_t*>(o0 + g * 68ull)[w] = reinterpret_cast<const uint32_t*>(src)[w];
+    }
+  } else {
+    unsigned char* o1 = reinterpret_cast<unsigned char*>(out1);
+    const int l0 = (int)(g & 1ull) < nw ? (int)(g & 1ull) : nw;
+    const int l1 = l0 + ((nw - l0) & ~1);
+    const unsigned char* isrc = buf + kWarpBatch * 96 + shift;
+    const uint4* v16 = reinterpret_cast<const uint4*>(buf);
+    uint4* dv = reinterpret_cast<uint4*>(o0 + g * 96ull);
+    for (int q = lane; q < nw * 6; q += 32) dv[q] = v16[q];
+    const uint4* i16 = reinterpret_cast<const uint4*>(isrc + (size_t)l0 * 24);
+    uint4* di = reinterpret_cast<uint4*>(o1 + (g + l0) * 24ull);
+    for (int q = lane; q < (l1 - l0) * 24 / 16; q += 32) di[q] = i16[q];
+    const int head = l0 * 6, tail = (nw - l1) * 6;
+    for (int q = lane; q < head + tail; q += 32) {
+      const int w = q < head ? q : (l1 * 6 + (q - head));
+      reinterpret_cast<uint32_t*>(o1 + g * 24ull)[w] = reinterpret_cast<const uint32_t*>(isrc)[w];
+    }
+  }
+}
+
 // A face of a warp's face list: local voxel (x, y, z) and emission direction.
 __device__ __forceinline__ uint32_t pack_face(int x, int y, int z, int d) {
   return (uint32_t)x | ((uint32_t)y << 7) | ((uint32_t)z << 14) | ((uint32_t)d << 21);
@@ -931,7 +971,8 @@ __device__ __forceinline__ int warp_faces(const ChunkSmem<N, LAYOUT>& s, bool us
 // chunk's generation).
 template <int N, int LAYOUT>
 __device__ void emit_chunk(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c, unsigned long long g0,
-                           unsigned long long cap, void* out0, void* out1, int nbuf) {
+                           unsigned long long cap, void* out0, void* out1, int nbuf,
+                           bool lane_flush) {
   constexpr int kBuf = warp_buf_bytes<LAYOUT>();
   const int nl = s.misc[1];
   const bool use_list = nl >= 0;
@@ -965,9 +1006,14 @@ __device__ void emit_chunk(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c, unsigned 
         stage_face<LAYOUT>(buf, kWarpBatch, shift, lane, d, (float)(ox + x), (float)(oy + y),
                            (float)(oz + z), first + (uint32_t)(r0 + lane), s.tab);
       }
-      fence_proxy_async_smem();
-      __syncwarp();
-      flush_warp<LAYOUT>(buf, shift, nw, g, out0, out1);
+      if (lane_flush) {
+        __syncwarp();
+        flush_warp_lanes<LAYOUT>(buf, shift, nw, g, out0, out1);
+      } else {
+        fence_proxy_async_smem();
+        __syncwarp();
+        flush_warp<LAYOUT>(buf, shift, nw, g, out0, out1);
+      }
       __syncwarp();
       b = nbuf == 2 ? b ^ 1 : 0;
     }
@@ -1132,7 +1178,8 @@ k_mesh_batch(MeshArgs a) {
     }
     __syncthreads();
     if (a.stage_faces > 0)
-      emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch);
+      emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch,
+                            a.lane_flush != 0);
     else emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1);
     if (threadIdx.x == 0) s_item = next_item;
     __syncthreads();
@@ -1330,7 +1377,8 @@ k_mesh_batch_phased(MeshArgs a) {
     __syncthreads();
     if (s_base == ~0ull) break;  // the scan flag never came: give up (error reported)
     if (a.stage_faces > 0)
-      emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch);
+      emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch,
+                            a.lane_flush != 0);
     else emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1);
     if (threadIdx.x == 0) s_item = next_item;
     __syncthreads();
@@ -1357,7 +1405,8 @@ k_mesh_single(MeshArgs a) {
     if ((unsigned long long)total > a.cap) atomicOr(&a.ctl->err, ERR_CAPACITY);
   }
   if (a.stage_faces > 0)
-    emit_chunk<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch);
+    emit_chunk<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch,
+                          a.lane_flush != 0);
   else emit_chunk_direct<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.out0, a.out1);
   if ((threadIdx.x & 31) == 0) bulk_wait_all();
 }

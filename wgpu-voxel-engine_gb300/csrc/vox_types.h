@@ -73,6 +73,7 @@ struct MeshArgs {
   int spin_limit;                    // polls before a look-back wait gives up
   uint32_t* scratch;                 // phased kernel: per-chunk occupancy + halo rows
   uint32_t* counts;                  // phased kernel: per-chunk face totals
+  int lane_flush;                    // staged faces leave shared memory by plain stores
 };
 
 }  // namespace vox
