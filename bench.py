@@ -59,6 +59,8 @@ def parse_args():
     p.add_argument("--plain-steps", type=int, default=3)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
+    p.add_argument("--no-graph", action="store_true",
+                   help="launch through vox_gen_mesh_batch instead of replaying captured graphs")
     p.add_argument("--tuning", default=None,
                    help="force a launch shape 'threads,stage_faces,ctas_per_sm[,schedule]' "
                         "(schedule 0 look-back, 1 phased; no autotune)")
@@ -282,7 +284,20 @@ def run_ours(args):
                                   chunk_index_base=wl.index_base + a, iters=args.tune_iters)
     tuning = ctx.tuning().as_dict() | {"autotuned": tuning is not None}
 
+    # each slab's launch captured once as a CUDA graph and replayed every step
+    graphs = []
+    if not args.no_graph:
+        with torch.cuda.stream(stream):
+            for si, (a, b) in enumerate(slabs):
+                graphs.append(ctx.capture_graph(d_coords[a:b], d_mask[a:b], b - a, o0, o1, cap,
+                                                d_offs[a + si:b + si + 1],
+                                                chunk_index_base=wl.index_base + a))
+
     def step():
+        if graphs:
+            for g in graphs:
+                g.launch()
+            return
         for si, (a, b) in enumerate(slabs):
             ctx.gen_mesh_batch(d_coords[a:b], d_mask[a:b], b - a, o0, o1, cap,
                                d_offs[a + si:b + si + 1], chunk_index_base=wl.index_base + a)
@@ -348,6 +363,8 @@ def run_ours(args):
         "config": {"workload": WORKLOAD_TEXT[args.workload], "chunks": n_all,
                    "chunk_size": cfg.chunk_size, "layout": args.layout,
                    "faces_per_step": total_faces, "launches_per_step": len(slabs),
+                   "launch": ("vox_gen_mesh_batch" if args.no_graph
+                              else "CUDA graph replay (one captured graph per slab)"),
                    "tuning": tuning,
                    "l2": "flushed before every step (256 MiB write, outside the events)",
                    "parallelism": f"dp{world} (independent chunk batches)"},

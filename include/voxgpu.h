@@ -259,6 +259,22 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
  * the context usable. */
 int vox_selftest_lookback_timeout(vox_ctx* ctx, int32_t spin_limit);
 
+/* ---- CUDA graph replay of the fused batch ---------------------------------------------- */
+
+/* One vox_gen_mesh_batch launch (same arguments, the context's tuning at capture time)
+ * captured as a CUDA graph. Replaces the per-tick dispatch of ChunkGenerator
+ * (src/chunk_builder.rs:69-132) when the same batch buffers are refilled every tick: the
+ * caller rewrites the contents of d_coords / d_nbr_mask in place and calls
+ * vox_graph_launch, which replays the launch on the context's stream without any
+ * per-launch host work. The graph owns its scratch; the context must outlive it.
+ * Device-side errors are latched in the context (vox_ctx_sync). */
+typedef struct vox_graph vox_graph;
+int vox_graph_capture(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
+                      int32_t n, int64_t chunk_index_base, void* d_out0, void* d_out1,
+                      uint64_t cap_faces, uint64_t* d_face_offsets, vox_graph** out);
+int vox_graph_launch(vox_graph* graph);
+int vox_graph_destroy(vox_graph* graph);
+
 /* Page-locked host memory for the host-pointer entry points (cudaMallocHost). */
 int vox_host_alloc(size_t bytes, void** out);
 int vox_host_free(void* p);

@@ -313,6 +313,46 @@ def test_host_entry_point_pinned_zero_copy(vox, oracle, schedule, layout):
     ctx.close()
 
 
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_graph_replay_with_inputs_rewritten_in_place(vox, oracle, schedule):
+    """A captured batch replays exactly; rewriting the inputs between replays changes the
+    result exactly as a fresh launch would, and other context calls in between do not
+    disturb the graph."""
+    wl = vox.workload("heightmap")
+    cfg = wl.config()
+    n = 256
+    sets = [list(wl.coords[:n]), list(wl.coords[n:2 * n]), list(wl.coords[:n])]
+    want = [oracle.gen_mesh_batch(cfg, c, vox.neighbour_masks(c)) for c in sets[:2]]
+    cap = max(int(w[2][-1]) for w in want)
+    ctx = ctx_for(vox, cfg)
+    use_schedule(ctx, schedule)
+    d_coords = to_dev(np.asarray(sets[0], np.int32))
+    d_mask = to_dev(np.asarray(vox.neighbour_masks(sets[0]), np.uint8))
+    o0, o1 = dev_bytes(cap * 96), dev_bytes(cap * 24)
+    offs = to_dev(np.zeros(n + 1, np.uint64))
+    g = ctx.capture_graph(d_coords, d_mask, n, o0, o1, cap, offs)
+    for k, coords in enumerate(sets):
+        d_coords.copy_(to_dev(np.asarray(coords, np.int32)))
+        d_mask.copy_(to_dev(np.asarray(vox.neighbour_masks(coords), np.uint8)))
+        for rep in range(2):
+            o0.fill_(0)
+            g.launch()
+            ctx.sync()
+            w0, w1, woffs = want[k % 2]
+            total = int(woffs[-1])
+            assert np.array_equal(to_np(offs), woffs), (k, rep)
+            assert np.array_equal(to_np(o0, total * 96), w0), (k, rep)
+            assert np.array_equal(to_np(o1, total * 24), w1), (k, rep)
+        # an ordinary launch on the same context between replays; the larger batch grows
+        # the context's own scratch (the graph keeps its own)
+        big = vox.grid_coords(range(0, 40), [0], range(0, 40))
+        ctx.gen_mesh_batch(to_dev(np.asarray(big, np.int32)), None, len(big), dev_bytes(16),
+                           dev_bytes(16), 0, to_dev(np.zeros(len(big) + 1, np.uint64)))
+        assert ctx.sync(raise_on_error=False) == vox.VOX_ERR_CAPACITY
+    g.close()
+    ctx.close()
+
+
 def test_host_entry_point_matches_oracle(vox, oracle):
     wl = vox.workload("plain")
     cfg = wl.config()

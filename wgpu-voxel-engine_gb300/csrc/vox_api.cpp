@@ -20,8 +20,7 @@
 
 using namespace vox;
 
-// Faces per warp staging buffer (the kernels' kWarpBatch).
-// staging windows of a warp: one 32-face buffer (32) or two (64)
+// Staging windows of a warp: one 32-face buffer (32) or two (64).
 constexpr int kStageSingle = 32;
 constexpr int kStageDouble = 64;
 
@@ -65,6 +64,21 @@ struct vox_ctx {
   void* d_out1 = nullptr;
   size_t out_cap_faces = 0;
   std::string last_error;
+};
+
+// One captured fused batch launch (vox_graph_capture). The graph owns the scratch of its
+// schedule, so later calls on the context never move a buffer the graph points at; the
+// queue/epoch/error word is the context's (launches on one stream never overlap).
+struct vox_graph {
+  vox_ctx* ctx = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int schedule = VOX_SCHEDULE_LOOKBACK;
+  unsigned long long* d_state = nullptr;  // look-back states (n)
+  uint32_t* d_scratch = nullptr;          // phased: occupancy + halo spill (n chunks)
+  uint32_t* d_counts = nullptr;           // phased: face totals (n)
+  size_t state_bytes = 0;
+  unsigned long long wiped_at = 0;        // context launch count when d_state was zeroed
 };
 
 namespace {
@@ -284,9 +298,9 @@ int check_outputs(vox_ctx* ctx, void* out0, void* out1, uint64_t cap) {
   return VOX_OK;
 }
 
-// host_out: the outputs are in host memory; the launch stages every warp's faces in one
-// shared-memory buffer and writes them out with plain full-line stores.
-int batch_launch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out = false) {
+// Issues one fused batch launch with the context's tuning on `stream`; the scratch of the
+// schedule (a.state, or a.scratch + a.counts) is already in `a`.
+int issue_batch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out, cudaStream_t stream) {
   const int layout = ctx->cfg.layout;
   const int threads = ctx->ks->threads[ctx->topt];
   const int smem = ctx->ks->smem_total(layout, threads, host_out ? kStageSingle : ctx->stage_faces);
@@ -294,29 +308,37 @@ int batch_launch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out = false) {
     a.stage_faces = kStageSingle;
     a.lane_flush = 1;
   }
+  void* params[] = {&a};
   if (ctx->schedule == VOX_SCHEDULE_PHASED) {
-    int st = ensure_scratch(ctx, (size_t)a.n);
-    if (st != VOX_OK) return st;
-    a.scratch = ctx->d_scratch;
-    a.counts = ctx->d_counts;
-    ++ctx->launches;
     const void* fn = ctx->ks->phased[gm][layout][ctx->topt];
     const int grid = std::max(1, std::min(a.n, host_out ? ctx->host_grid[gm] : ctx->phased_grid[gm]));
-    void* params[] = {&a};
     VOX_CUDA(ctx, cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), params, (size_t)smem,
-                                              ctx->stream),
+                                              stream),
              "cudaLaunchCooperativeKernel");
     return VOX_OK;
   }
-  int st = ensure_state(ctx, (size_t)a.n);
-  if (st != VOX_OK) return st;
-  st = before_batch_launch(ctx);
-  if (st != VOX_OK) return st;
-  a.state = ctx->d_state;
   const void* fn = ctx->ks->batch[gm][layout][ctx->topt];
   const int grid = std::max(1, std::min(a.n, host_out ? ctx->host_grid[gm] : ctx->batch_grid[gm]));
-  void* params[] = {&a};
-  return launch(ctx, fn, grid, threads, smem, params);
+  VOX_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(threads), params, (size_t)smem, stream),
+           "cudaLaunchKernel");
+  return VOX_OK;
+}
+
+// host_out: the outputs are in host memory; the launch stages every warp's faces in one
+// shared-memory buffer and writes them out with plain full-line stores.
+int batch_launch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out = false) {
+  int st;
+  if (ctx->schedule == VOX_SCHEDULE_PHASED) {
+    if ((st = ensure_scratch(ctx, (size_t)a.n)) != VOX_OK) return st;
+    a.scratch = ctx->d_scratch;
+    a.counts = ctx->d_counts;
+    ++ctx->launches;
+  } else {
+    if ((st = ensure_state(ctx, (size_t)a.n)) != VOX_OK) return st;
+    if ((st = before_batch_launch(ctx)) != VOX_OK) return st;
+    a.state = ctx->d_state;
+  }
+  return issue_batch(ctx, a, gm, host_out, ctx->stream);
 }
 
 }  // namespace
@@ -863,6 +885,102 @@ int vox_selftest_lookback_timeout(vox_ctx* ctx, int32_t spin_limit) {
   const int st = e == cudaSuccess ? sync_locked(ctx) : cuda_fail(ctx, e, "lookback probe");
   cudaFree(words);
   return st;
+}
+
+static void graph_free(vox_graph* g) {
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  cudaFree(g->d_state);
+  cudaFree(g->d_scratch);
+  cudaFree(g->d_counts);
+  delete g;
+}
+
+int vox_graph_capture(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
+                      int32_t n, int64_t chunk_index_base, void* d_out0, void* d_out1,
+                      uint64_t cap_faces, uint64_t* d_face_offsets, vox_graph** out) {
+  if (!ctx || !out) return VOX_ERR_INVALID;
+  *out = nullptr;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (n <= 0 || !d_coords || !d_face_offsets) return fail(ctx, VOX_ERR_INVALID, "bad arguments");
+  int st = check_outputs(ctx, d_out0, d_out1, cap_faces);
+  if (st != VOX_OK) return st;
+  vox_graph* g = new (std::nothrow) vox_graph();
+  if (!g) return VOX_ERR_OOM;
+  g->ctx = ctx;
+  g->schedule = ctx->schedule;
+  auto bail = [&](int s) {
+    graph_free(g);
+    return s;
+  };
+  cudaError_t e;
+  MeshArgs a = base_args(ctx);
+  a.n = n;
+  a.index_base = chunk_index_base;
+  a.coords = d_coords;
+  a.nbr_mask = d_nbr_mask;
+  a.out0 = d_out0;
+  a.out1 = d_out1;
+  a.cap = cap_faces;
+  a.face_offsets = reinterpret_cast<unsigned long long*>(d_face_offsets);
+  if (g->schedule == VOX_SCHEDULE_PHASED) {
+    if ((e = cudaMalloc(&g->d_scratch, (size_t)n * (size_t)ctx->ks->spill_bytes)) != cudaSuccess ||
+        (e = cudaMalloc(&g->d_counts, (size_t)n * sizeof(uint32_t))) != cudaSuccess)
+      return bail(cuda_fail(ctx, e, "cudaMalloc(graph scratch)"));
+    a.scratch = g->d_scratch;
+    a.counts = g->d_counts;
+  } else {
+    g->state_bytes = (size_t)n * sizeof(unsigned long long);
+    if ((e = cudaMalloc(&g->d_state, g->state_bytes)) != cudaSuccess ||
+        (e = cudaMemsetAsync(g->d_state, 0, g->state_bytes, ctx->stream)) != cudaSuccess)
+      return bail(cuda_fail(ctx, e, "cudaMalloc(graph state)"));
+    g->wiped_at = ctx->launches;
+    a.state = g->d_state;
+  }
+  // Capture on a private stream (thread-local mode: other threads' CUDA calls are not
+  // affected), then replay on the context's stream.
+  cudaStream_t cs = nullptr;
+  if ((e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess)
+    return bail(cuda_fail(ctx, e, "cudaStreamCreate(capture)"));
+  if ((e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+    cudaStreamDestroy(cs);
+    return bail(cuda_fail(ctx, e, "cudaStreamBeginCapture"));
+  }
+  st = issue_batch(ctx, a, ctx->gm, false, cs);
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(cs, &graph);
+  cudaStreamDestroy(cs);
+  g->graph = graph;
+  if (st != VOX_OK) return bail(st);
+  if (e != cudaSuccess) return bail(cuda_fail(ctx, e, "cudaStreamEndCapture"));
+  if ((e = cudaGraphInstantiate(&g->exec, g->graph, 0)) != cudaSuccess)
+    return bail(cuda_fail(ctx, e, "cudaGraphInstantiate"));
+  if ((e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
+    return bail(cuda_fail(ctx, e, "cudaStreamSynchronize"));
+  *out = g;
+  return VOX_OK;
+}
+
+int vox_graph_launch(vox_graph* g) {
+  if (!g || !g->ctx) return VOX_ERR_INVALID;
+  vox_ctx* ctx = g->ctx;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ++ctx->launches;
+  // look-back states carry a 24-bit launch epoch: zero them before a tag can repeat
+  if (g->d_state && ctx->launches - g->wiped_at >= (1ull << 23)) {
+    VOX_CUDA(ctx, cudaMemsetAsync(g->d_state, 0, g->state_bytes, ctx->stream), "cudaMemsetAsync(state)");
+    g->wiped_at = ctx->launches;
+  }
+  VOX_CUDA(ctx, cudaGraphLaunch(g->exec, ctx->stream), "cudaGraphLaunch");
+  return VOX_OK;
+}
+
+int vox_graph_destroy(vox_graph* g) {
+  if (!g) return VOX_OK;
+  if (g->ctx && g->ctx->stream) cudaStreamSynchronize(g->ctx->stream);
+  graph_free(g);
+  return VOX_OK;
 }
 
 int vox_host_alloc(size_t bytes, void** out) {

@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import weakref
 from dataclasses import dataclass
 
 from . import _build
@@ -134,6 +135,10 @@ _SIGS = {
     "vox_autotune": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, ctypes.c_int64, _P, _P,
                                     ctypes.c_uint64, _P, ctypes.c_int32, ctypes.POINTER(Tuning)]),
     "vox_selftest_lookback_timeout": (ctypes.c_int, [_P, ctypes.c_int32]),
+    "vox_graph_capture": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, ctypes.c_int64, _P, _P,
+                                         ctypes.c_uint64, _P, ctypes.POINTER(_P)]),
+    "vox_graph_launch": (ctypes.c_int, [_P]),
+    "vox_graph_destroy": (ctypes.c_int, [_P]),
     "vox_serve_create": (ctypes.c_int, [ctypes.POINTER(ServeConfig), ctypes.POINTER(_P)]),
     "vox_serve_destroy": (ctypes.c_int, [_P]),
     "vox_serve_now": (ctypes.c_double, []),
@@ -231,9 +236,12 @@ class Context:
             raise VoxError(st, "vox_ctx_create")
         self._h = h
         self.sizes = query_sizes(cfg)
+        self._graphs = weakref.WeakSet()
 
     def close(self):
         if getattr(self, "_h", None):
+            for g in list(getattr(self, "_graphs", ())):
+                g.close()  # a graph needs its context
             self._lib.vox_ctx_destroy(self._h)
             self._h = None
 
@@ -329,10 +337,44 @@ class Context:
     def selftest_lookback_timeout(self, spin_limit: int) -> int:
         return self._lib.vox_selftest_lookback_timeout(self._h, spin_limit)
 
+    def capture_graph(self, d_coords, d_nbr_mask, n: int, d_out0, d_out1, cap_faces: int,
+                      d_offsets, chunk_index_base: int = 0) -> "Graph":
+        """vox_graph_capture: one fused batch launch captured as a CUDA graph."""
+        h = _P()
+        self._check(self._lib.vox_graph_capture(self._h, _ptr(d_coords), _ptr(d_nbr_mask), n,
+                                                chunk_index_base, _ptr(d_out0), _ptr(d_out1),
+                                                cap_faces, _ptr(d_offsets), ctypes.byref(h)),
+                    "vox_graph_capture")
+        g = Graph(self, h)
+        self._graphs.add(g)
+        return g
+
     def frustum_cull(self, planes, d_coords, n: int, d_visible):
         p = (ctypes.c_float * 24)(*[float(v) for v in planes])
         self._check(self._lib.vox_frustum_cull(self._h, ctypes.addressof(p), _ptr(d_coords), n,
                                                _ptr(d_visible)), "vox_frustum_cull")
+
+
+class Graph:
+    """A captured fused batch launch (vox_graph_*); replays on its context's stream."""
+
+    def __init__(self, ctx: "Context", handle):
+        self._ctx = ctx
+        self._h = handle
+
+    def launch(self):
+        self._ctx._check(self._ctx._lib.vox_graph_launch(self._h), "vox_graph_launch")
+
+    def close(self):
+        if self._h:
+            self._ctx._lib.vox_graph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def camera_matrix(eye, direction, aspect=16 / 9, fovy=1.0471976, znear=0.1, zfar=1000.0):
