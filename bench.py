@@ -353,7 +353,7 @@ def run_ours(args):
     alg_bytes = total_faces * (b0 + b1) + n_all * (12 + 1) + (n_all + len(slabs)) * 8
     kernel_ms = statistics.median(step_ms)
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
-    kname = "k_mesh_batch"
+    kname = "k_mesh_batch_phased" if tuning.get("schedule") == "phased" else "k_mesh_batch"
     traffic = profiled_traffic(kname, args.workload)
     line = {
         "metric": METRIC, "value": value, "unit": "chunks/s", "n_gpus": world,

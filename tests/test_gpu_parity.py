@@ -32,6 +32,14 @@ def gen_cfg(vox, kind, n, layout=0, cull=0):
         return vox.make_config(chunk_size=n, layout=layout, cull_mode=cull, kind=vox.GEN_DENSITY,
                                octaves=3, seed=1234, frequency=1 / 96, y_ref=float(n // 2),
                                y_scale=1 / 64)
+    if kind == "density6":  # more octaves than the lattice-table path takes (per-sample path)
+        return vox.make_config(chunk_size=n, layout=layout, cull_mode=cull, kind=vox.GEN_DENSITY,
+                               octaves=6, seed=77, frequency=1 / 40, y_ref=float(n // 2),
+                               y_scale=1 / 32)
+    if kind == "densityhf":  # too many lattice corners for the tables (per-sample path)
+        return vox.make_config(chunk_size=n, layout=layout, cull_mode=cull, kind=vox.GEN_DENSITY,
+                               octaves=2, seed=5, frequency=0.7, y_ref=float(n // 2),
+                               y_scale=1 / 16)
     if kind == "refdensity":  # the reference's parameters and fill rule (noise < 0 -> solid)
         return vox.make_config(chunk_size=n, layout=layout, cull_mode=cull, kind=vox.GEN_DENSITY,
                                octaves=3, seed=1, frequency=0.09, lacunarity=0.5, gain=2.5,
@@ -41,7 +49,8 @@ def gen_cfg(vox, kind, n, layout=0, cull=0):
 
 
 @pytest.mark.parametrize("n", [8, 16, 32, 64])
-@pytest.mark.parametrize("kind", ["height", "height1", "density", "refdensity", "bernoulli"])
+@pytest.mark.parametrize("kind", ["height", "height1", "density", "density6", "densityhf",
+                                  "refdensity", "bernoulli"])
 def test_generate_matches_oracle(vox, oracle, n, kind):
     cfg = gen_cfg(vox, kind, n)
     coords = small_coords()

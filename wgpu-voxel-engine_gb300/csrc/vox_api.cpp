@@ -312,6 +312,8 @@ int issue_batch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out, cudaStream_t s
   if (ctx->schedule == VOX_SCHEDULE_PHASED) {
     const void* fn = ctx->ks->phased[gm][layout][ctx->topt];
     const int grid = std::max(1, std::min(a.n, host_out ? ctx->host_grid[gm] : ctx->phased_grid[gm]));
+    // emission items per chunk: one, unless there are fewer chunks than CTAs
+    a.split = std::max(1, std::min(8, grid / a.n));
     VOX_CUDA(ctx, cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), params, (size_t)smem,
                                               stream),
              "cudaLaunchCooperativeKernel");
@@ -480,12 +482,11 @@ static int sync_locked(vox_ctx* ctx) {
   VOX_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
   const unsigned err = ctx->h_ctl->err;
   if (err == 0) return VOX_OK;
-  // Clear the error bits. After a timeout a phased launch may have left its queues and
-  // its barrier count mid-way: reset them too (the epoch and generation words stay).
+  // Clear the error bits. After a timeout a phased launch may have left its queue and its
+  // barrier count mid-way: reset them too (the epoch and generation words stay).
   ctx->h_ctl->err = 0;
   if (err & ERR_TIMEOUT) {
     ctx->h_ctl->next = 0;
-    ctx->h_ctl->next2 = 0;
     ctx->h_ctl->bar_count = 0;
   }
   VOX_CUDA(ctx, cudaMemcpyAsync(ctx->d_ctl, ctx->h_ctl, sizeof(BatchCtl), cudaMemcpyHostToDevice,

@@ -57,6 +57,22 @@ struct AxisZ {
 
 // Octaves whose per-axis lattice data are computed between one pair of barriers.
 constexpr int kOctGroup = 8;
+
+// Density generation from per-chunk lattice tables (see dens_tables): per octave and axis
+// the lattice data of the N + 2 coordinates (local -1..N), and the gradient coefficients
+// of every lattice corner the chunk's coordinates touch. Configurations beyond these
+// limits (more octaves, more corners, frequencies <= 0) take the per-sample hash path.
+struct DensAxis {
+  int ci;                  // lattice cell relative to the chunk's first cell on this axis
+  float fr, fade, fr1;     // fractional coordinate, its fade, fractional - 1
+};
+constexpr int kDensMaxOct = 4;
+template <int N>
+__host__ __device__ constexpr int dens_max_corners() { return N <= 8 ? 128 : (N <= 16 ? 256 : 1024); }
+template <int N>
+__host__ __device__ constexpr int dens_scratch_bytes() {
+  return 64 + kDensMaxOct * 3 * (N + 2) * 16 + dens_max_corners<N>() * 16;
+}
 // Faces one warp's 32 voxels can have (6 each): the size of a warp's face list.
 constexpr int kWarpFaces = 32 * 6;
 // Faces one warp stages at a time (each warp has two staging buffers of this many faces).
@@ -81,6 +97,9 @@ struct SmemPlan {
   static constexpr int kVList = align16(Shape<N>::VCap * 2);
   static constexpr int kMisc = 64;
   static constexpr int kFixed0 = kTables + kOcc + kHalo + kRows + kNz + kVList + kMisc;
+  // the chunk state from occ through misc (contiguous in shared memory), as spilled by the
+  // phased kernel: occupancy, halo, row offsets, row and voxel lists, counts
+  static constexpr int kSpill = kOcc + kHalo + kRows + kNz + kVList + kMisc;
   // per-warp face lists (face-parallel emission)
   __host__ __device__ static int list_bytes(int threads) { return (threads / 32) * kWarpFaces * 4; }
   __host__ __device__ static int fixed(int threads) { return kFixed0 + list_bytes(threads); }
@@ -88,7 +107,8 @@ struct SmemPlan {
   static constexpr int kColK = align16((N + 2) * (N + 2) * 4);
   static constexpr int kAxisHalf = kOctGroup * align16((N + 2) * 16);
   static constexpr int kAxis = 2 * kAxisHalf;
-  static constexpr int kGenScratch = kColK + kAxis;
+  static constexpr int kGenScratch =
+      kColK + kAxis > dens_scratch_bytes<N>() ? kColK + kAxis : dens_scratch_bytes<N>();
   // staging area: stage_faces / kWarpBatch buffers per warp when staging (stage_faces
   // 32 or 64), else only the generation scratch
   __host__ __device__ static int stage_bytes(int threads, int stage_faces) {
@@ -496,6 +516,134 @@ __device__ __forceinline__ bool gen_solid(const ChunkSmem<N, LAYOUT>& s, const G
   }
 }
 
+// Builds the density lattice tables of a chunk in the generation scratch (all threads; ends
+// with a barrier) and returns true, or returns false without a barrier when the
+// configuration is beyond the table limits (the same answer in every thread).
+// Scratch layout: int hdr[16] (per octave: corner-table base, corners along y and along
+// z), DensAxis axes[octave][axis][N + 2], float4 corners[...].
+template <int N, int LAYOUT, int T>
+__device__ bool dens_tables(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, int oy, int oz) {
+  if (g.octaves > kDensMaxOct) return false;
+  int* hdr = reinterpret_cast<int*>(s.stage);
+  DensAxis* axes = reinterpret_cast<DensAxis*>(s.stage + 64);
+  float4* corners = reinterpret_cast<float4*>(s.stage + 64 + kDensMaxOct * 3 * (N + 2) * 16);
+  const int org[3] = {ox, oy, oz};
+  // corner counts (every thread computes them; cheap)
+  int lo[kDensMaxOct][3], nc[kDensMaxOct][3], base[kDensMaxOct];
+  int total = 0;
+  float f = g.freq;
+#pragma unroll
+  for (int o = 0; o < kDensMaxOct; ++o) {
+    if (o < g.octaves) {
+      if (!(f > 0.0f)) return false;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        // coordinates grow with the local index (f > 0): local -1 has the first cell, N the last
+        const int c0 = (int)floorf((float)(org[a] - 1) * f);
+        const int c1 = (int)floorf((float)(org[a] + N) * f);
+        lo[o][a] = c0;
+        nc[o][a] = c1 - c0 + 2;  // corners along this axis
+      }
+      base[o] = total;
+      total += nc[o][0] * nc[o][1] * nc[o][2];
+      f = f * g.lac;
+    }
+  }
+  if (total > dens_max_corners<N>()) return false;
+  const int t = threadIdx.x;
+  if (t < g.octaves) {
+    hdr[4 * t + 0] = base[t];
+    hdr[4 * t + 1] = nc[t][1];
+    hdr[4 * t + 2] = nc[t][2];
+  }
+  // axis data: the oracle's per-sample operations, once per coordinate
+  for (int i = t; i < g.octaves * 3 * (N + 2); i += T) {
+    const int o = i / (3 * (N + 2)), r = i % (3 * (N + 2));
+    const int a = r / (N + 2), k = r % (N + 2);
+    float fo = g.freq;
+    for (int q = 0; q < o; ++q) fo = fo * g.lac;
+    const float c = (float)(org[a] + k - 1) * fo;
+    const float fl = floorf(c);
+    DensAxis v;
+    v.fr = c - fl;
+    v.fade = d_fade(v.fr);
+    v.fr1 = v.fr - 1.0f;
+    int c0 = 0;
+#pragma unroll
+    for (int q = 0; q < kDensMaxOct; ++q)
+#pragma unroll
+      for (int b = 0; b < 3; ++b)
+        if (q == o && b == a) c0 = lo[q][b];
+    v.ci = (int)fl - c0;
+    axes[i] = v;
+  }
+  // corner gradients: hash p[p[p[X] + Y] + Z] of the corner's lattice coordinates mod 256
+  // (the doubled permutation makes this the hash the per-sample chain computes)
+  const uint8_t* p = s.tab->perm;
+  const float4* gt = reinterpret_cast<const float4*>(s.tab->grad);
+  for (int i = t; i < total; i += T) {
+    int o = 0;
+#pragma unroll
+    for (int q = 1; q < kDensMaxOct; ++q)
+      if (q < g.octaves && i >= base[q]) o = q;
+    int ix = 0, iy = 0, iz = 0, l0 = 0, l1 = 0, l2 = 0, n1 = 1, n2 = 1, b0 = 0;
+#pragma unroll
+    for (int q = 0; q < kDensMaxOct; ++q)
+      if (q == o) {
+        b0 = base[q];
+        n1 = nc[q][1];
+        n2 = nc[q][2];
+        l0 = lo[q][0];
+        l1 = lo[q][1];
+        l2 = lo[q][2];
+      }
+    const int j = i - b0;
+    iz = j % n2;
+    iy = (j / n2) % n1;
+    ix = j / (n1 * n2);
+    const int X = (l0 + ix) & 255, Y = (l1 + iy) & 255, Z = (l2 + iz) & 255;
+    corners[i] = gt[p[p[p[X] + Y] + Z] & 15];
+  }
+  __syncthreads();
+  return true;
+}
+
+// Density test of local sample (x, y, z), -1 <= x, y, z <= N, from the lattice tables:
+// the operations of the per-sample path (d_fbm3 + the density rule), in the same order.
+template <int N, int LAYOUT>
+__device__ __forceinline__ bool dens_solid_tab(const ChunkSmem<N, LAYOUT>& s, const GenDev& g,
+                                               int x, int y, int z, int oy) {
+  const int* hdr = reinterpret_cast<const int*>(s.stage);
+  const DensAxis* axes = reinterpret_cast<const DensAxis*>(s.stage + 64);
+  const float4* corners = reinterpret_cast<const float4*>(s.stage + 64 + kDensMaxOct * 3 * (N + 2) * 16);
+  float sum = 0.0f, amp = 1.0f;
+  for (int o = 0; o < g.octaves; ++o) {
+    const DensAxis* ao = axes + o * 3 * (N + 2);
+    const DensAxis ax = ao[x + 1], ay = ao[(N + 2) + y + 1], az = ao[2 * (N + 2) + z + 1];
+    const int n1 = hdr[4 * o + 1], n2 = hdr[4 * o + 2];
+    const int sx = n1 * n2;
+    const float4* C = corners + hdr[4 * o] + (ax.ci * n1 + ay.ci) * n2 + az.ci;
+    const float4 g000 = C[0], g100 = C[sx], g010 = C[n2], g110 = C[sx + n2];
+    const float4 g001 = C[1], g101 = C[sx + 1], g011 = C[n2 + 1], g111 = C[sx + n2 + 1];
+    const float xf = ax.fr, yf = ay.fr, zf = az.fr, x1 = ax.fr1, y1 = ay.fr1, z1 = az.fr1;
+    const float u = ax.fade, v = ay.fade, w = az.fade;
+    const float l00 = d_lerp(u, (g000.x * xf + g000.y * yf) + g000.z * zf,
+                             (g100.x * x1 + g100.y * yf) + g100.z * zf);
+    const float l10 = d_lerp(u, (g010.x * xf + g010.y * y1) + g010.z * zf,
+                             (g110.x * x1 + g110.y * y1) + g110.z * zf);
+    const float l01 = d_lerp(u, (g001.x * xf + g001.y * yf) + g001.z * z1,
+                             (g101.x * x1 + g101.y * yf) + g101.z * z1);
+    const float l11 = d_lerp(u, (g011.x * xf + g011.y * y1) + g011.z * z1,
+                             (g111.x * x1 + g111.y * y1) + g111.z * z1);
+    const float n = d_lerp(w, d_lerp(v, l00, l10), d_lerp(v, l01, l11));
+    sum = sum + amp * n;
+    amp = amp * g.gain;
+  }
+  const int wy = oy + y;
+  const float d = sum - ((float)wy - g.y_ref) * g.y_scale;
+  return g.solid_below_zero ? (d < 0.0f) : (d > 0.0f);
+}
+
 // Fills s.occ (own rows) and, for every set bit of `halo_mask`, the halo rows; the other
 // halo rows are zero (a neighbour that is not loaded counts as air, chunk.rs:102-107).
 template <int N, int GM, int LAYOUT, int T>
@@ -510,11 +658,13 @@ __device__ void gen_chunk(ChunkSmem<N, LAYOUT>& s, const GenDev& g, vox_chunk_co
   const unsigned long long s0 = g.seed ^ (unsigned long long)chunk_index;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   uint32_t* occw = reinterpret_cast<uint32_t*>(s.occ);
+  const bool tab = GM == GM_DENSITY && dens_tables<N, LAYOUT, T>(s, g, ox, oy, oz);
   for (int base = warp * 32; base < N * N * N; base += nwarps * 32) {
     const int e = base + lane;
     const int row = e / N, x = e % N;
     const int y = row / N, z = row % N;
-    store_ballot<N>(occw, e, gen_solid<N, GM, LAYOUT>(s, g, x, y, z, ox, oy, oz, s0));
+    store_ballot<N>(occw, e, tab ? dens_solid_tab<N, LAYOUT>(s, g, x, y, z, oy)
+                                 : gen_solid<N, GM, LAYOUT>(s, g, x, y, z, ox, oy, oz, s0));
   }
   if (with_halo) {
     uint32_t* halow = reinterpret_cast<uint32_t*>(s.halo);
@@ -525,7 +675,8 @@ __device__ void gen_chunk(ChunkSmem<N, LAYOUT>& s, const GenDev& g, vox_chunk_co
           int x, y, z;
           halo_coord<N>(h, e / N, e % N, x, y, z);
           store_ballot<N>(halow + h * N * Shape<N>::W, e,
-                          gen_solid<N, GM, LAYOUT>(s, g, x, y, z, ox, oy, oz, s0));
+                          tab ? dens_solid_tab<N, LAYOUT>(s, g, x, y, z, oy)
+                              : gen_solid<N, GM, LAYOUT>(s, g, x, y, z, ox, oy, oz, s0));
         }
       } else {
         for (int i = threadIdx.x; i < N; i += blockDim.x) s.halo[h * N + i] = (RowT)0;
@@ -932,10 +1083,9 @@ __device__ __forceinline__ int warp_faces(const ChunkSmem<N, LAYOUT>& s, bool us
 #pragma unroll
     for (int d = 0; d < 6; ++d) bits |= (unsigned)((m[d] >> x) & (RowT)1) << d;
     // Only lane 0's position is needed (the warp scan places the others): the row's face
-    // offset plus the faces of the voxels before x in the row. Row by row, a warp starts
-    // on a row boundary (x = 0) unless rows are 64 wide (x = 0 or 32).
+    // offset plus the faces of the voxels before x in the row.
     uint32_t pre = 0;
-    if ((use_list || N > 32) && lane == 0 && x != 0) {
+    if (lane == 0 && x != 0) {
       const RowT below = (RowT)(~(RowT)0) >> (sizeof(RowT) * 8 - x);
 #pragma unroll
       for (int d = 0; d < 6; ++d) pre += (uint32_t)popc_row(m[d] & below);
@@ -961,6 +1111,13 @@ __device__ __forceinline__ int warp_faces(const ChunkSmem<N, LAYOUT>& s, bool us
   return total;
 }
 
+// Emission elements of the chunk in shared memory: listed face voxels, or every voxel of
+// the rows with faces.
+template <int N, int LAYOUT>
+__device__ __forceinline__ int emit_elems(const ChunkSmem<N, LAYOUT>& s) {
+  return s.misc[1] >= 0 ? s.misc[1] : s.misc[0] * N;
+}
+
 // Emits the faces of the chunk in reference order: chunk-local face f goes to global
 // face g0 + f. Every warp compacts the faces of its 32 voxels, stages them 32 at a time
 // in one of its two shared-memory buffers (one face record per lane, final byte layout)
@@ -969,54 +1126,68 @@ __device__ __forceinline__ int warp_faces(const ChunkSmem<N, LAYOUT>& s, bool us
 // bulk copy that last read a buffer is done before refilling it, and until all its
 // copies have read shared memory at the end (the staging area is reused by the next
 // chunk's generation).
+// Sends the nwf faces of a warp's face list (chunk-local indices first, first + 1, ...) to
+// global faces g0 + first + ...: 32 at a time staged in one of the warp's nbuf buffers
+// (`bufs`, buffer index b carried across calls) and sent by a TMA bulk copy, or by
+// coalesced lane stores when lane_flush.
+template <int N, int LAYOUT>
+__device__ __forceinline__ void warp_send_faces(const TablesDev* tab, const uint32_t* list, int nwf,
+                                                uint32_t first, vox_chunk_coord c,
+                                                unsigned long long g0, unsigned long long cap,
+                                                void* out0, void* out1, unsigned char* bufs,
+                                                int nbuf, bool lane_flush, int& b) {
+  constexpr int kBuf = warp_buf_bytes<LAYOUT>();
+  const int ox = c.x * N, oy = c.y * N, oz = c.z * N;
+  const int lane = threadIdx.x & 31;
+  for (int r0 = 0; r0 < nwf; r0 += kWarpBatch) {
+    const int cnt = nwf - r0 < kWarpBatch ? nwf - r0 : kWarpBatch;
+    const unsigned long long g = g0 + first + (unsigned)r0;
+    int nw = cnt;
+    if (g >= cap) nw = 0;
+    else if (g + (unsigned long long)cnt > cap) nw = (int)(cap - g);
+    if (nw == 0) continue;
+    unsigned char* buf = bufs + b * kBuf;
+    // the copy issued nbuf batches ago read this buffer; wait until it is done reading
+    if (lane == 0) {
+      if (nbuf == 1) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+      else asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
+    }
+    __syncwarp();
+    const int shift = stage_shift<LAYOUT>(g);
+    if (lane < nw) {
+      const uint32_t q = list[r0 + lane];
+      const int x = q & 127, y = (q >> 7) & 127, z = (q >> 14) & 127, d = q >> 21;
+      stage_face<LAYOUT>(buf, kWarpBatch, shift, lane, d, (float)(ox + x), (float)(oy + y),
+                         (float)(oz + z), first + (uint32_t)(r0 + lane), tab);
+    }
+    if (lane_flush) {
+      __syncwarp();
+      flush_warp_lanes<LAYOUT>(buf, shift, nw, g, out0, out1);
+    } else {
+      fence_proxy_async_smem();
+      __syncwarp();
+      flush_warp<LAYOUT>(buf, shift, nw, g, out0, out1);
+    }
+    __syncwarp();
+    b = nbuf == 2 ? b ^ 1 : 0;
+  }
+}
+
 template <int N, int LAYOUT>
 __device__ void emit_chunk(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c, unsigned long long g0,
                            unsigned long long cap, void* out0, void* out1, int nbuf,
-                           bool lane_flush) {
+                           bool lane_flush, int lo, int hi) {
   constexpr int kBuf = warp_buf_bytes<LAYOUT>();
-  const int nl = s.misc[1];
-  const bool use_list = nl >= 0;
-  const int elems = use_list ? nl : s.misc[0] * N;
-  const int ox = c.x * N, oy = c.y * N, oz = c.z * N;
+  const bool use_list = s.misc[1] >= 0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   uint32_t* list = s.lists + warp * kWarpFaces;
   unsigned char* bufs = s.stage + (size_t)warp * nbuf * kBuf;
   int b = 0;
-  for (int base = warp * 32; base < elems; base += nwarps * 32) {
+  for (int base = lo + warp * 32; base < hi; base += nwarps * 32) {
     uint32_t first;
-    const int nwf = warp_faces<N, LAYOUT>(s, use_list, elems, base, list, first);
-    for (int r0 = 0; r0 < nwf; r0 += kWarpBatch) {
-      const int cnt = nwf - r0 < kWarpBatch ? nwf - r0 : kWarpBatch;
-      const unsigned long long g = g0 + first + (unsigned)r0;
-      int nw = cnt;
-      if (g >= cap) nw = 0;
-      else if (g + (unsigned long long)cnt > cap) nw = (int)(cap - g);
-      if (nw == 0) continue;
-      unsigned char* buf = bufs + b * kBuf;
-      // the copy issued nbuf batches ago read this buffer; wait until it is done reading
-      if (lane == 0) {
-        if (nbuf == 1) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-        else asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory");
-      }
-      __syncwarp();
-      const int shift = stage_shift<LAYOUT>(g);
-      if (lane < nw) {
-        const uint32_t q = list[r0 + lane];
-        const int x = q & 127, y = (q >> 7) & 127, z = (q >> 14) & 127, d = q >> 21;
-        stage_face<LAYOUT>(buf, kWarpBatch, shift, lane, d, (float)(ox + x), (float)(oy + y),
-                           (float)(oz + z), first + (uint32_t)(r0 + lane), s.tab);
-      }
-      if (lane_flush) {
-        __syncwarp();
-        flush_warp_lanes<LAYOUT>(buf, shift, nw, g, out0, out1);
-      } else {
-        fence_proxy_async_smem();
-        __syncwarp();
-        flush_warp<LAYOUT>(buf, shift, nw, g, out0, out1);
-      }
-      __syncwarp();
-      b = nbuf == 2 ? b ^ 1 : 0;
-    }
+    const int nwf = warp_faces<N, LAYOUT>(s, use_list, hi, base, list, first);
+    warp_send_faces<N, LAYOUT>(s.tab, list, nwf, first, c, g0, cap, out0, out1, bufs, nbuf,
+                               lane_flush, b);
   }
   if (lane == 0) bulk_wait_read_all();
   __syncwarp();
@@ -1064,29 +1235,37 @@ __device__ __forceinline__ void store_face(void* out0, void* out1, unsigned long
 // Direct variant of emit_chunk: no staging window and no barrier; after the same
 // face compaction every lane writes one face record straight to global memory, so the
 // 32 lanes of a warp write 32 consecutive faces.
+// The direct counterpart of warp_send_faces: lane l stores faces l, l + 32, ... of the
+// list straight to global memory.
+template <int N, int LAYOUT>
+__device__ __forceinline__ void warp_store_faces(const TablesDev* tab, const uint32_t* list, int nwf,
+                                                 uint32_t first, vox_chunk_coord c,
+                                                 unsigned long long g0, unsigned long long cap,
+                                                 void* out0, void* out1) {
+  const int ox = c.x * N, oy = c.y * N, oz = c.z * N;
+  for (int i = threadIdx.x & 31; i < nwf; i += 32) {
+    const uint32_t q = list[i];
+    const int x = q & 127, y = (q >> 7) & 127, z = (q >> 14) & 127, d = q >> 21;
+    const uint32_t l = first + (uint32_t)i;
+    const unsigned long long gg = g0 + l;
+    if (gg < cap)
+      store_face<LAYOUT>(out0, out1, gg, d, (float)(ox + x), (float)(oy + y), (float)(oz + z),
+                         l, tab);
+  }
+  __syncwarp();
+}
+
 template <int N, int LAYOUT>
 __device__ void emit_chunk_direct(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c,
                                   unsigned long long g0, unsigned long long cap, void* out0,
-                                  void* out1) {
-  const int nl = s.misc[1];
-  const bool use_list = nl >= 0;
-  const int elems = use_list ? nl : s.misc[0] * N;
-  const int ox = c.x * N, oy = c.y * N, oz = c.z * N;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+                                  void* out1, int lo, int hi) {
+  const bool use_list = s.misc[1] >= 0;
+  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   uint32_t* list = s.lists + warp * kWarpFaces;
-  for (int base = warp * 32; base < elems; base += nwarps * 32) {
+  for (int base = lo + warp * 32; base < hi; base += nwarps * 32) {
     uint32_t first;
-    const int nwf = warp_faces<N, LAYOUT>(s, use_list, elems, base, list, first);
-    for (int i = lane; i < nwf; i += 32) {
-      const uint32_t q = list[i];
-      const int x = q & 127, y = (q >> 7) & 127, z = (q >> 14) & 127, d = q >> 21;
-      const uint32_t l = first + (uint32_t)i;
-      const unsigned long long gg = g0 + l;
-      if (gg < cap)
-        store_face<LAYOUT>(out0, out1, gg, d, (float)(ox + x), (float)(oy + y), (float)(oz + z),
-                           l, s.tab);
-    }
-    __syncwarp();
+    const int nwf = warp_faces<N, LAYOUT>(s, use_list, hi, base, list, first);
+    warp_store_faces<N, LAYOUT>(s.tab, list, nwf, first, c, g0, cap, out0, out1);
   }
 }
 
@@ -1179,8 +1358,8 @@ k_mesh_batch(MeshArgs a) {
     __syncthreads();
     if (a.stage_faces > 0)
       emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch,
-                            a.lane_flush != 0);
-    else emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1);
+                            a.lane_flush != 0, 0, emit_elems(s));
+    else emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, 0, emit_elems(s));
     if (threadIdx.x == 0) s_item = next_item;
     __syncthreads();
     i = s_item;
@@ -1292,7 +1471,13 @@ template <int N, int GM, int LAYOUT, int T>
 __global__ void __launch_bounds__(T)
 k_mesh_batch_phased(MeshArgs a) {
   using P = SmemPlan<N, LAYOUT>;
-  constexpr int kSpill16 = (P::kOcc + P::kHalo) / 16;  // occupancy + halo rows, in uint4
+  // spill slot of a chunk: [occ | halo | rows] [nz] [vlist] [misc], laid out as in shared
+  // memory; the lists are copied only as far as they are used
+  constexpr int kFixed16 = (P::kOcc + P::kHalo + P::kRows) / 16;
+  constexpr int kNzOff = P::kOcc + P::kHalo + P::kRows;
+  constexpr int kVlOff = kNzOff + P::kNz;
+  constexpr int kMiscOff = kVlOff + P::kVList;
+  static_assert(P::kSpill == kMiscOff + P::kMisc, "spill layout");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ChunkSmem<N, LAYOUT> s;
   s.carve(smem_raw);
@@ -1300,21 +1485,30 @@ k_mesh_batch_phased(MeshArgs a) {
   __shared__ int s_item;
   __shared__ unsigned s_gen;
   __shared__ unsigned long long s_base;
-  uint4* const spill = reinterpret_cast<uint4*>(a.scratch);
-  uint4* const occ16 = reinterpret_cast<uint4*>(s.occ);  // s.halo follows s.occ
+  unsigned char* const spill = reinterpret_cast<unsigned char*>(a.scratch);
+  uint4* const fixed16 = reinterpret_cast<uint4*>(s.occ);  // s.halo, s.rows follow s.occ
+  const int t = threadIdx.x;
   __syncthreads();
 
   // A. prepare + count + spill (the next ticket is drawn before the chunk's work)
-  if (threadIdx.x == 0) s_item = (int)atomicAdd(&a.ctl->next, 1u);
+  if (t == 0) s_item = (int)atomicAdd(&a.ctl->next, 1u);
   __syncthreads();
   for (int i = s_item; i < a.n;) {
     int next_item = 0;
-    if (threadIdx.x == 0) next_item = (int)atomicAdd(&a.ctl->next, 1u);
+    if (t == 0) next_item = (int)atomicAdd(&a.ctl->next, 1u);
     prepare_chunk<N, GM, LAYOUT, T>(s, a, i, a.coords[i]);
     const uint32_t total = count_and_scan<N, LAYOUT, T>(s);
-    uint4* dst = spill + (unsigned long long)i * kSpill16;
-    for (int k = threadIdx.x; k < kSpill16; k += T) __stcg(dst + k, occ16[k]);
-    if (threadIdx.x == 0) {
+    unsigned char* dst = spill + (unsigned long long)i * P::kSpill;
+    for (int q = t; q < kFixed16; q += T) __stcg(reinterpret_cast<uint4*>(dst) + q, fixed16[q]);
+    const int nzw = (s.misc[0] + 1) >> 1;                          // u32 words of nz used
+    const int vlw = s.misc[1] > 0 ? (s.misc[1] + 1) >> 1 : 0;      // u32 words of vlist used
+    for (int q = t; q < nzw; q += T)
+      __stcg(reinterpret_cast<uint32_t*>(dst + kNzOff) + q, reinterpret_cast<const uint32_t*>(s.nz)[q]);
+    for (int q = t; q < vlw; q += T)
+      __stcg(reinterpret_cast<uint32_t*>(dst + kVlOff) + q,
+             reinterpret_cast<const uint32_t*>(s.vlist)[q]);
+    if (t == 0) {
+      __stcg(reinterpret_cast<int2*>(dst + kMiscOff), make_int2(s.misc[0], s.misc[1]));
       __stcg(a.counts + i, total);
       s_item = next_item;
     }
@@ -1324,7 +1518,7 @@ k_mesh_batch_phased(MeshArgs a) {
 
   // B. barrier; CTA 0 scans the counts
   __syncthreads();
-  if (threadIdx.x == 0) s_gen = grid_barrier_t0(a.ctl, gridDim.x, a.spin_limit);
+  if (t == 0) s_gen = grid_barrier_t0(a.ctl, gridDim.x, a.spin_limit);
   __syncthreads();
   const unsigned gen = s_gen;
   if (gen == 0xFFFFFFFFu) return;
@@ -1332,32 +1526,51 @@ k_mesh_batch_phased(MeshArgs a) {
     const unsigned long long total = scan_counts<T>(a.counts, a.n, a.face_offsets,
                                                     reinterpret_cast<unsigned long long*>(s.stage));
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (t == 0) {
       if (total > a.cap) atomicOr(&a.ctl->err, ERR_CAPACITY);
       __threadfence();
       st_release_u32(&a.ctl->scan_flag, gen);
     }
   }
 
-  // C. reload + recount + emit
+  // C. emission items from the work queue: item k is segment k % split of chunk
+  // k / split (the chunk's emission elements cut into split runs of whole warp batches).
+  // The chunk state comes back from the spill slot, so nothing is counted twice.
+  const int split = a.split > 0 ? a.split : 1;
+  const int items = a.n * split;
   bool scanned = blockIdx.x == 0;  // thread 0's view: the scan flag has been seen
-  if (threadIdx.x == 0) s_item = (int)atomicAdd(&a.ctl->next2, 1u);
+  if (t == 0) s_item = (int)atomicAdd(&a.ctl->next, 1u);
   __syncthreads();
-  int i = s_item;
+  int k = s_item;
   while (true) {
-    if (i >= a.n) {
-      // The last ticket of this launch resets the second queue.
-      if (threadIdx.x == 0 && i == a.n + (int)gridDim.x - 1) a.ctl->next2 = 0u;
+    if (k >= items) {
+      // The last ticket of this launch resets the queue.
+      if (t == 0 && k == items + (int)gridDim.x - 1) a.ctl->next = 0u;
       break;
     }
     int next_item = 0;
-    if (threadIdx.x == 0) next_item = (int)atomicAdd(&a.ctl->next2, 1u);
-    const vox_chunk_coord c = a.coords[i];
-    const uint4* src = spill + (unsigned long long)i * kSpill16;
-    for (int k = threadIdx.x; k < kSpill16; k += T) occ16[k] = __ldcg(src + k);
+    if (t == 0) next_item = (int)atomicAdd(&a.ctl->next, 1u);
+    const int i = k / split, seg = k - i * split;
+    const unsigned char* src = spill + (unsigned long long)i * P::kSpill;
+    for (int q = t; q < kFixed16; q += T) fixed16[q] = __ldcg(reinterpret_cast<const uint4*>(src) + q);
+    if (t == 0) {
+      const int2 m = __ldcg(reinterpret_cast<const int2*>(src + kMiscOff));
+      s.misc[0] = m.x;
+      s.misc[1] = m.y;
+    }
     __syncthreads();
-    count_and_scan<N, LAYOUT, T>(s);
-    if (threadIdx.x == 0) {
+    const bool use_list = s.misc[1] >= 0;
+    const int elems = emit_elems(s);
+    const int per = ((elems + split - 1) / split + 31) & ~31;
+    const int lo = min(elems, seg * per), hi = min(elems, lo + per);
+    if (lo < hi) {
+      // the list entries that elements [lo, hi) read
+      const int e0 = use_list ? lo : lo / N, e1 = use_list ? hi : (hi - 1) / N + 1;
+      const uint32_t* lsrc = reinterpret_cast<const uint32_t*>(src + (use_list ? kVlOff : kNzOff));
+      uint32_t* ldst = reinterpret_cast<uint32_t*>(use_list ? s.vlist : s.nz);
+      for (int q = (e0 >> 1) + t; q < (e1 + 1) >> 1; q += T) ldst[q] = __ldcg(lsrc + q);
+    }
+    if (t == 0) {
       int spins = 0;
       while (!scanned) {
         if (ld_acquire_u32(&a.ctl->scan_flag) == gen) {
@@ -1376,15 +1589,18 @@ k_mesh_batch_phased(MeshArgs a) {
     }
     __syncthreads();
     if (s_base == ~0ull) break;  // the scan flag never came: give up (error reported)
-    if (a.stage_faces > 0)
-      emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch,
-                            a.lane_flush != 0);
-    else emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1);
-    if (threadIdx.x == 0) s_item = next_item;
+    if (lo < hi) {
+      const vox_chunk_coord c = a.coords[i];
+      if (a.stage_faces > 0)
+        emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch,
+                              a.lane_flush != 0, lo, hi);
+      else emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, lo, hi);
+    }
+    if (t == 0) s_item = next_item;
     __syncthreads();
-    i = s_item;
+    k = s_item;
   }
-  if ((threadIdx.x & 31) == 0) bulk_wait_all();  // every lane 0 issued bulk copies
+  if ((t & 31) == 0) bulk_wait_all();  // every lane 0 issued bulk copies
 }
 
 // Plain per-chunk mesher: one chunk, one CTA, one launch (no queue, no look-back).
@@ -1406,8 +1622,8 @@ k_mesh_single(MeshArgs a) {
   }
   if (a.stage_faces > 0)
     emit_chunk<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch,
-                          a.lane_flush != 0);
-  else emit_chunk_direct<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.out0, a.out1);
+                          a.lane_flush != 0, 0, emit_elems(s));
+  else emit_chunk_direct<N, LAYOUT>(s, a.coord_single, 0ull, a.cap, a.out0, a.out1, 0, emit_elems(s));
   if ((threadIdx.x & 31) == 0) bulk_wait_all();
 }
 

@@ -40,7 +40,7 @@ static KernelSet make_kernel_set() {
   k.single[1][0] = (const void*)k_mesh_single<N, VOX_LAYOUT_INSTANCED, Shape<N>::T0>;
   k.single[1][1] = (const void*)k_mesh_single<N, VOX_LAYOUT_INSTANCED, Shape<N>::T1>;
   k.gen_threads = Shape<N>::T1;
-  k.spill_bytes = SmemPlan<N, VOX_LAYOUT_VERTEX>::kOcc + SmemPlan<N, VOX_LAYOUT_VERTEX>::kHalo;
+  k.spill_bytes = SmemPlan<N, VOX_LAYOUT_VERTEX>::kSpill;
   k.generate[0] = nullptr;
   k.generate[GM_HEIGHT] = (const void*)k_generate<N, GM_HEIGHT, Shape<N>::T1>;
   k.generate[GM_DENSITY] = (const void*)k_generate<N, GM_DENSITY, Shape<N>::T1>;

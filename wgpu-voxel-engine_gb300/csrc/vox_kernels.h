@@ -13,7 +13,7 @@ struct KernelSet {
   const void* single[2][2];     // k_mesh_single<N, layout, threads[t]>
   const void* generate[4];      // k_generate<N, gen mode, gen_threads> (index 0 unused)
   int gen_threads;
-  int spill_bytes;              // occupancy + halo rows of one chunk (phased scratch)
+  int spill_bytes;              // chunk state of one chunk (phased scratch)
   // dynamic shared memory of a launch (layout, CTA size, staging window in faces)
   int (*smem_total)(int layout, int threads, int stage_faces);
 };

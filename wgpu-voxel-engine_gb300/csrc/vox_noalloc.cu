@@ -90,7 +90,7 @@ k_mesh_batch_noalloc(const __grid_constant__ MeshArgs a, const __grid_constant__
       }
     }
     __syncthreads();
-    emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1);
+    emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, 0, emit_elems(s));
     __syncthreads();
   }
 }

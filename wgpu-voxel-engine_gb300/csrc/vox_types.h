@@ -41,11 +41,10 @@ struct BatchCtl {
   unsigned int next;       // work-queue ticket; reset to 0 by the last CTA of a launch
   unsigned int epoch;      // look-back state tag; advanced by the last CTA of a launch
   unsigned int err;        // ERR_* bits, sticky until the host clears them
-  unsigned int next2;      // second work-queue ticket (emission phase of the phased kernel)
   unsigned int bar_count;  // grid barrier: CTAs arrived (reset by the last arriver)
   unsigned int bar_gen;    // grid barrier: generation, advanced by the last arriver
   unsigned int scan_flag;  // phased kernel: the generation whose offset scan is complete
-  unsigned int pad;
+  unsigned int pad[2];
 };
 
 struct MeshArgs {
@@ -71,7 +70,8 @@ struct MeshArgs {
   int full6;
   int stage_faces;                   // faces per staging window (0: direct global stores)
   int spin_limit;                    // polls before a look-back wait gives up
-  uint32_t* scratch;                 // phased kernel: per-chunk occupancy + halo rows
+  uint32_t* scratch;                 // phased kernel: per-chunk spilled chunk state
+  int split;                         // phased kernel: emission segments per chunk
   uint32_t* counts;                  // phased kernel: per-chunk face totals
   int lane_flush;                    // staged faces leave shared memory by plain stores
 };
