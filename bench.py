@@ -164,11 +164,41 @@ def profiled_traffic(kernel: str, workload: str):
     return None
 
 
-def cpu_baseline(wl, cfg, masks, seconds: float):
-    """The oracle restatement of the reference CPU chunk builder on all host threads,
-    repeated over the workload (or a prefix of it) for about `seconds`."""
+# FP32 operations of one noise sample-octave in the noise formula (the oracle's
+# or_noise2_f32 / or_noise3_f32 plus one fBm step): floors, fractional parts, fades
+# (7 each), corner gradients (2-D: 2 mul + 1 add; 3-D: 3 mul + 2 add), lerps (3 each),
+# the coordinate scaling and the fBm update (sum, amp, f).
+NOISE_OPS = {2: 2 + 2 + 14 + 2 + 4 * 3 + 3 * 3 + 2 + 4, 3: 3 + 3 + 21 + 3 + 8 * 5 + 7 * 3 + 3 + 4}
+# FP32 instruction rate with FMA contraction off (one op per instruction): 152 SMs x 128
+# lanes x 2.07 GHz. Nominal: the measured peaks file has no FP32 figure.
+FP32_OPS_NOMINAL = 152 * 128 * 2.07e9
+
+
+def noise_report(wl, cfg, n_chunks, ms_per_step):
+    """Algorithmic FP32 throughput of the noise in one step: samples x octaves x ops."""
+    N = cfg.chunk_size
+    g = cfg.gen
+    if g.kind == 0:    # heightmap: 2-D noise per column, (N + 2)^2 - 4 columns with halo
+        samples, dim = (N + 2) ** 2 - 4, 2
+    elif g.kind == 1:  # density: 3-D noise per voxel and halo voxel
+        samples, dim = N ** 3 + 6 * N * N, 3
+    else:
+        return None
+    ops = n_chunks * samples * g.octaves * NOISE_OPS[dim]
+    achieved = ops / (ms_per_step / 1e3)
+    return {"samples_per_chunk": samples, "octaves": g.octaves, "ops_per_sample_octave": NOISE_OPS[dim],
+            "achieved_tops": achieved / 1e12, "peak_tops": FP32_OPS_NOMINAL / 1e12,
+            "peak_source": "nominal FP32 instruction rate (FMA contraction off)",
+            "frac": achieved / FP32_OPS_NOMINAL,
+            "note": "the fused launch also culls and emits; this is the noise share of the step's "
+                    "time budget, not the noise kernel alone"}
+
+
+def cpu_baseline(wl, cfg, masks, seconds: float, threads: int = 0):
+    """The oracle restatement of the reference CPU chunk builder on `threads` host threads
+    (0: all), repeated over the workload (or a prefix of it) for about `seconds`."""
     import vox_oracle
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     coords = list(wl.coords)
     # calibrate on a small prefix, then size the sample to the time budget
     k = min(len(coords), 64)
@@ -386,8 +416,13 @@ def run_ours(args):
         # p50/p99 request-to-mesh latency of the streaming engine at the serving request
         # rate (real-time 60 frames/s camera), next to the batch throughput above
         line["latency"] = serving_run(args.latency_frames, paced=True)
+    noise = noise_report(wl, cfg, n_all, ms_per_step)
+    if noise:
+        line["noise_fp32"] = noise
     if rank == 0 and world == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(wl, cfg, masks, args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(wl, cfg, masks, args.cpu_seconds * 0.75)
+        line["cpu_baseline_single_thread"] = cpu_baseline(wl, cfg, masks, args.cpu_seconds * 0.25,
+                                                          threads=1)
     if rank == 0:
         print(json.dumps(line), flush=True)
     ctx.close()

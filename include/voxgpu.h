@@ -13,6 +13,8 @@
  *   ChunkGenerator (pool closure)       src/chunk_builder.rs:80-84 -> vox_gen_mesh_batch
  *   Frustum::matrix_to_planes           src/frustum_culling.rs:47-85 -> vox_frustum_planes
  *   Frustum::contains                   src/frustum_culling.rs:16-40 -> vox_frustum_cull
+ *   World::render (draw loop)           src/world.rs:24-40        -> vox_draw_list
+ *   ChunkGenerator per-tick dispatch    src/chunk_builder.rs:69-132 -> vox_graph_capture/launch
  *
  * Conventions
  *  - Every call returns an int status (VOX_OK = 0, see vox_status).
@@ -289,6 +291,26 @@ int vox_frustum_planes(const float m_colmajor[16], float planes[24]);
  * planes (src/frustum_culling.rs:16-40), with the AABB edge = chunk_size. */
 int vox_frustum_cull(vox_ctx* ctx, const float planes[24], const vox_chunk_coord* d_coords,
                      int32_t n, uint8_t* d_visible);
+
+/* One indexed indirect draw (the layout of wgpu's DrawIndexedIndirectArgs), 20 bytes. */
+typedef struct vox_draw_indexed_indirect {
+  uint32_t index_count;
+  uint32_t instance_count;
+  uint32_t first_index;
+  int32_t base_vertex;
+  uint32_t first_instance;
+} vox_draw_indexed_indirect;
+
+/* World::render (src/world.rs:24-40) as a draw list: for every chunk i of a meshed batch
+ * (d_face_offsets: its n + 1 offsets) that passes the vox_frustum_cull test and has faces,
+ * one record in d_draws, in chunk order; *d_count receives the number of records.
+ * Vertex layout: {6 * faces, 1, 6 * face_offsets[i], 4 * face_offsets[i], 0} (the indices
+ * are chunk-local). Instanced layout: {6, faces, 0, 0, face_offsets[i]} over the quad's
+ * six indices. d_draws needs room for n records. Offsets beyond the 32-bit fields latch
+ * VOX_ERR_CAPACITY (vox_ctx_sync) and zero the record. */
+int vox_draw_list(vox_ctx* ctx, const float planes[24], const vox_chunk_coord* d_coords,
+                  const uint64_t* d_face_offsets, int32_t n, vox_draw_indexed_indirect* d_draws,
+                  uint32_t* d_count);
 
 #ifdef __cplusplus
 }

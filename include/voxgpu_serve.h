@@ -68,6 +68,24 @@ double vox_serve_now(void);
  * the engine sees its batch finished); does not wait for the GPU. */
 int vox_serve_frame(vox_serve* s, const float view_proj[16], const float eye[3], double now_s);
 
+/* Explicit requests (the reference's ChunkGenerator enqueue, chunk_builder.rs:54-66,
+ * without the camera): requests every chunk of coords[0..n) that is neither pending nor
+ * resident, refreshes the others, writes each chunk's request id to ids_out (may be NULL)
+ * and admits what fits. A chunk keeps its id while it is pending or resident. */
+int vox_serve_submit(vox_serve* s, const vox_chunk_coord* coords, int32_t n, double now_s,
+                     uint64_t* ids_out);
+
+/* Request states. UNKNOWN: never issued, or evicted since. */
+enum { VOX_REQ_UNKNOWN = 0, VOX_REQ_PENDING = 1, VOX_REQ_RESIDENT = 2 };
+
+/* Integrates finished batches, admits queued requests and reports the request's state. */
+int vox_serve_poll(vox_serve* s, uint64_t id, int32_t* state);
+
+/* Drives the engine until request `id` is resident (VOX_OK), or returns VOX_ERR_TIMEOUT
+ * after timeout_s seconds, VOX_ERR_INVALID for an unknown id, VOX_ERR_OOM if the cache
+ * budget cannot hold its batch. */
+int vox_serve_wait(vox_serve* s, uint64_t id, double timeout_s);
+
 /* Waits for every batch in flight (and every queued request) and integrates them. */
 int vox_serve_drain(vox_serve* s);
 

@@ -405,6 +405,38 @@ def test_frustum_matches_oracle(vox, oracle):
     ctx.close()
 
 
+@pytest.mark.parametrize("layout", LAYOUTS)
+def test_draw_list_matches_oracle(vox, oracle, layout):
+    """World::render as an indirect draw list: the visible chunks with faces, in chunk
+    order, with the vertex / instance ranges of their meshes."""
+    from test_oracle_kat import perspective_look
+    wl = vox.workload("heightmap")
+    cfg = wl.config(layout=layout)
+    coords = list(wl.coords[:600])
+    masks = vox.neighbour_masks(coords)
+    _, _, offs = oracle.gen_mesh_batch(cfg, coords, masks)
+    eye = (100.0, 40.0, 60.0)
+    m = perspective_look(eye, (1.0, -0.3, 0.4))
+    planes = oracle.frustum_planes(m)
+    want = []
+    for i, c in enumerate(coords):
+        f0, nf = int(offs[i]), int(offs[i + 1]) - int(offs[i])
+        if nf > 0 and oracle.frustum_contains(planes, c, 16):
+            want.append((6, nf, 0, 0, f0) if layout == 1 else (6 * nf, 1, 6 * f0, 4 * f0, 0))
+    assert 0 < len(want) < len(coords)
+    ctx = ctx_for(vox, cfg)
+    d_draws = to_dev(np.zeros((len(coords), 5), np.uint32))
+    d_count = to_dev(np.zeros(1, np.uint32))
+    ctx.draw_list(planes, to_dev(np.asarray(coords, np.int32)), to_dev(offs), len(coords),
+                  d_draws, d_count)
+    ctx.sync()
+    k = int(to_np(d_count)[0])
+    got = to_np(d_draws)[:k].astype(np.int64)
+    assert k == len(want)
+    assert np.array_equal(got, np.asarray(want, np.int64).reshape(-1, 5))
+    ctx.close()
+
+
 def test_invalid_arguments_rejected(vox):
     cfg = vox.make_config(chunk_size=16)
     ctx = ctx_for(vox, cfg)

@@ -84,3 +84,30 @@ def test_serving_evicts_lru_under_budget(vox):
     assert st.cache_bytes <= budget
     assert st.completed >= st.requested - st.pending
     server.close()
+
+
+def test_submit_poll_wait_by_request_id(vox, oracle):
+    """Explicit requests: ids are stable per chunk, wait returns when resident, the mesh is
+    the chunk's final mesh, and unknown ids are reported as such."""
+    wl = vox.workload("heightmap")
+    cfg = wl.config()
+    server = vox.Server(cfg, view_radius=4, max_batch=8, slots=2)
+    coords = [(3, 0, -2), (4, 0, -2), (-7, 0, 9), (0, 0, 0), (11, 0, 5)]
+    ids = server.submit(coords)
+    assert len(set(ids)) == len(coords) and all(i > 0 for i in ids)
+    assert server.submit(coords[:2]) == ids[:2]  # the same chunks keep their ids
+    assert server.poll(10 ** 9) == vox.VOX_REQ_UNKNOWN
+    assert server.wait(10 ** 9, 1.0) == vox.VOX_ERR_INVALID
+    for c, i in zip(coords, ids):
+        assert server.poll(i) in (vox.VOX_REQ_PENDING, vox.VOX_REQ_RESIDENT)
+        assert server.wait(i, 30.0) == vox.VOX_OK
+        assert server.poll(i) == vox.VOX_REQ_RESIDENT
+        p0, p1, faces = server.lookup(c)
+        # the engine generates every lateral halo: the chunk's mesh with all four present
+        w0, w1, woffs = oracle.gen_mesh_batch(cfg, [c], [0x0F])
+        assert faces == int(woffs[-1])
+        assert np.array_equal(fetch(p0, faces * 96), w0)
+        assert np.array_equal(fetch(p1, faces * 24), w1)
+    st = server.stats()
+    assert st.requested == len(coords) and st.completed == len(coords)
+    server.close()

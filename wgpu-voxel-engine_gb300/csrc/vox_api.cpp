@@ -772,6 +772,22 @@ int vox_frustum_cull(vox_ctx* ctx, const float planes[24], const vox_chunk_coord
   return VOX_OK;
 }
 
+int vox_draw_list(vox_ctx* ctx, const float planes[24], const vox_chunk_coord* d_coords,
+                  const uint64_t* d_face_offsets, int32_t n, vox_draw_indexed_indirect* d_draws,
+                  uint32_t* d_count) {
+  if (!ctx) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (!planes || !d_count || n < 0 || (n > 0 && (!d_coords || !d_face_offsets || !d_draws)))
+    return fail(ctx, VOX_ERR_INVALID, "bad arguments");
+  Planes pl;
+  std::memcpy(pl.p, planes, sizeof pl.p);
+  VOX_CUDA(ctx, launch_draw_list(pl, d_coords, reinterpret_cast<const unsigned long long*>(d_face_offsets),
+                                 n, ctx->cfg.chunk_size, ctx->cfg.layout == VOX_LAYOUT_INSTANCED ? 1 : 0,
+                                 d_draws, d_count, &ctx->d_ctl->err, ctx->stream),
+           "draw list");
+  return VOX_OK;
+}
+
 int vox_ctx_get_tuning(vox_ctx* ctx, vox_tuning* out) {
   if (!ctx || !out) return VOX_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->mu);

@@ -3,6 +3,8 @@
 
 #include <cuda_runtime.h>
 
+#include "voxgpu.h"
+
 namespace vox {
 
 struct KernelSet {
@@ -33,6 +35,10 @@ struct Planes {
 };
 cudaError_t launch_frustum(const Planes& planes, const void* coords, int n, int extent,
                            uint8_t* visible, cudaStream_t st);
+using DrawRecord = vox_draw_indexed_indirect;
+cudaError_t launch_draw_list(const Planes& planes, const void* coords,
+                             const unsigned long long* offs, int n, int extent, int instanced,
+                             DrawRecord* out, uint32_t* count, unsigned* err, cudaStream_t st);
 
 struct BatchCtl;
 // One look-back for chunk 1 of a batch whose chunk 0 never publishes: the wait must give

@@ -1,9 +1,11 @@
-// vox_misc.cu — small kernels around the hot path: the chunk-frustum test and the
-// conversions between occupancy bitmasks and the reference's one-byte-per-voxel cubes.
+// vox_misc.cu — small kernels around the hot path: the chunk-frustum test, the indirect
+// draw list of the visible meshes, and the conversions between occupancy bitmasks and the
+// reference's one-byte-per-voxel cubes.
 #include <cstdint>
 
 #include "voxgpu.h"
 #include "vox_kernels.h"
+#include "vox_types.h"
 
 namespace vox {
 
@@ -50,14 +52,10 @@ __global__ void k_cubes_to_occ(const uint8_t* __restrict__ cubes, long long word
 // Frustum::contains (src/frustum_culling.rs:16-40) per chunk: corners in the reference's
 // order, planes near, far, left, right, top, bottom; dist = ((a*x + b*y) + c*z) + d with
 // one rounding per operation (the file is built with -fmad=false).
-__global__ void k_frustum(Planes pl, const vox_chunk_coord* __restrict__ coords, int n, int extent,
-                          uint8_t* __restrict__ visible) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const vox_chunk_coord c = coords[i];
+__device__ __forceinline__ bool frustum_contains(const Planes& pl, vox_chunk_coord c, int extent) {
   const float px = (float)(c.x * extent), py = (float)(c.y * extent), pz = (float)(c.z * extent);
   const float e = (float)extent;
-  uint8_t inside_any = 0;
+  bool inside_any = false;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     const float x = (k & 1) ? px + e : px;
@@ -69,9 +67,83 @@ __global__ void k_frustum(Planes pl, const vox_chunk_coord* __restrict__ coords,
       const float d = pl.p[4 * j] * x + pl.p[4 * j + 1] * y + pl.p[4 * j + 2] * z + pl.p[4 * j + 3];
       inside = inside && !(d < 0.0f);
     }
-    inside_any |= inside ? 1 : 0;
+    inside_any = inside_any || inside;
   }
-  visible[i] = inside_any;
+  return inside_any;
+}
+
+__global__ void k_frustum(Planes pl, const vox_chunk_coord* __restrict__ coords, int n, int extent,
+                          uint8_t* __restrict__ visible) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  visible[i] = frustum_contains(pl, coords[i], extent) ? 1 : 0;
+}
+
+// World::render (src/world.rs:24-40) as an indirect draw list: one CTA walks the chunks
+// in tiles of 1024, tests each (Frustum::contains), and compacts the visible chunks that
+// have faces in chunk order (warp ballots, then a scan of the 32 warp totals). Records
+// whose counts or offsets do not fit the 32-bit fields latch ERR_CAPACITY and are zeroed.
+__global__ void __launch_bounds__(1024)
+k_draw_list(Planes pl, const vox_chunk_coord* __restrict__ coords,
+            const unsigned long long* __restrict__ offs, int n, int extent, int instanced,
+            DrawRecord* __restrict__ out, uint32_t* __restrict__ count, unsigned* err) {
+  __shared__ uint32_t wsum[32];
+  __shared__ uint32_t s_total;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  uint32_t base = 0;
+  for (int tile = 0; tile < n; tile += 1024) {
+    const int i = tile + t;
+    bool vis = false;
+    unsigned long long f0 = 0, nf = 0;
+    if (i < n) {
+      f0 = offs[i];
+      nf = offs[i + 1] - f0;
+      vis = nf > 0 && frustum_contains(pl, coords[i], extent);
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, vis);
+    const uint32_t before = (uint32_t)__popc(bal & ((1u << lane) - 1u));
+    if (lane == 0) wsum[warp] = (uint32_t)__popc(bal);
+    __syncthreads();
+    if (warp == 0) {
+      const uint32_t v = wsum[lane];
+      uint32_t incl = v;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t u = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += u;
+      }
+      wsum[lane] = incl - v;
+      if (lane == 31) s_total = incl;
+    }
+    __syncthreads();
+    if (vis) {
+      DrawRecord r;
+      bool fits;
+      if (instanced) {  // the quad's 6 indices, one instance per face
+        fits = f0 + nf <= 0xFFFFFFFFull;
+        r.index_count = 6u;
+        r.instance_count = (uint32_t)nf;
+        r.first_index = 0u;
+        r.base_vertex = 0;
+        r.first_instance = (uint32_t)f0;
+      } else {          // 6 indices per face, chunk-local indices over 4 vertices per face
+        fits = 6ull * (f0 + nf) <= 0xFFFFFFFFull && 4ull * f0 <= 0x7FFFFFFFull;
+        r.index_count = (uint32_t)(6ull * nf);
+        r.instance_count = 1u;
+        r.first_index = (uint32_t)(6ull * f0);
+        r.base_vertex = (int32_t)(4ull * f0);
+        r.first_instance = 0u;
+      }
+      if (!fits) {
+        atomicOr(err, ERR_CAPACITY);
+        r = DrawRecord{0u, 0u, 0u, 0, 0u};
+      }
+      out[base + wsum[warp] + before] = r;
+    }
+    base += s_total;
+    __syncthreads();
+  }
+  if (t == 0) *count = base;
 }
 
 int grid_for(long long work, int threads) {
@@ -104,6 +176,14 @@ cudaError_t launch_frustum(const Planes& planes, const void* coords, int n, int 
   if (n == 0) return cudaSuccess;
   k_frustum<<<(n + 255) / 256, 256, 0, st>>>(planes, static_cast<const vox_chunk_coord*>(coords),
                                               n, extent, visible);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_draw_list(const Planes& planes, const void* coords,
+                             const unsigned long long* offs, int n, int extent, int instanced,
+                             DrawRecord* out, uint32_t* count, unsigned* err, cudaStream_t st) {
+  k_draw_list<<<1, 1024, 0, st>>>(planes, static_cast<const vox_chunk_coord*>(coords), offs, n,
+                                  extent, instanced, out, count, err);
   return cudaGetLastError();
 }
 

@@ -15,6 +15,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -53,6 +54,7 @@ struct Block {
 
 struct Entry {
   enum State { PENDING, RESIDENT } state = PENDING;
+  uint64_t id = 0;  // request id (vox_serve_submit / poll / wait)
   double requested_at = 0.0;
   uint64_t last_seen = 0;
   std::shared_ptr<Block> block;
@@ -97,6 +99,8 @@ struct vox_serve {
   vox_chunk_coord center{0, 0, 0};
   // state
   std::unordered_map<vox_chunk_coord, Entry, CoordHash, CoordEq> entries;
+  std::unordered_map<uint64_t, vox_chunk_coord> by_id;  // request id -> chunk
+  uint64_t next_id = 1;
   std::vector<vox_chunk_coord> queue;
   std::vector<double> latencies;
   vox_serve_stats stats{};
@@ -150,6 +154,7 @@ bool make_room(vox_serve* s, uint64_t need) {
     }
     if (victim == s->entries.end()) return false;
     release(s, victim->second);
+    s->by_id.erase(victim->second.id);
     s->entries.erase(victim);
     ++s->stats.evicted;
     --s->stats.resident;
@@ -235,6 +240,28 @@ int integrate(vox_serve* s, Slot& sl, double now) {
   sl.block.reset();
   sl.chunks.clear();
   return VOX_OK;
+}
+
+// Requests chunk c (or refreshes it when already pending or resident) and returns its
+// request id.
+uint64_t request(vox_serve* s, const vox_chunk_coord& c, double now_s) {
+  auto it = s->entries.find(c);
+  if (it != s->entries.end()) {
+    it->second.last_seen = s->frame;
+    return it->second.id;
+  }
+  Entry e;
+  e.state = Entry::PENDING;
+  e.id = s->next_id++;
+  e.requested_at = now_s;
+  e.last_seen = s->frame;
+  s->entries.emplace(c, e);
+  s->by_id.emplace(e.id, c);
+  s->queue.push_back(c);
+  ++s->stats.requested;
+  ++s->stats.pending;
+  if (s->first_request < 0.0) s->first_request = now_s;
+  return e.id;
 }
 
 int poll_and_admit(vox_serve* s, bool wait) {
@@ -394,24 +421,53 @@ int vox_serve_frame(vox_serve* s, const float view_proj[16], const float eye[3],
           cudaSuccess ||
       cudaStreamSynchronize(s->cull_stream) != cudaSuccess)
     return VOX_ERR_CUDA;
-  for (int i = 0; i < n; ++i) {
-    if (!s->h_vis[i]) continue;
-    auto it = s->entries.find(s->cand[i]);
-    if (it != s->entries.end()) {
-      it->second.last_seen = s->frame;
-      continue;
-    }
-    Entry e;
-    e.state = Entry::PENDING;
-    e.requested_at = now_s;
-    e.last_seen = s->frame;
-    s->entries.emplace(s->cand[i], e);
-    s->queue.push_back(s->cand[i]);
-    ++s->stats.requested;
-    ++s->stats.pending;
-    if (s->first_request < 0.0) s->first_request = now_s;
+  for (int i = 0; i < n; ++i)
+    if (s->h_vis[i]) request(s, s->cand[i], now_s);
+  return poll_and_admit(s, false);
+}
+
+int vox_serve_submit(vox_serve* s, const vox_chunk_coord* coords, int32_t n, double now_s,
+                     uint64_t* ids_out) {
+  if (!s || n < 0 || (n > 0 && !coords)) return VOX_ERR_INVALID;
+  if (now_s < 0.0) now_s = mono_now();
+  for (int32_t i = 0; i < n; ++i) {
+    const uint64_t id = request(s, coords[i], now_s);
+    if (ids_out) ids_out[i] = id;
   }
   return poll_and_admit(s, false);
+}
+
+static int32_t request_state(vox_serve* s, uint64_t id) {
+  auto it = s->by_id.find(id);
+  if (it == s->by_id.end()) return VOX_REQ_UNKNOWN;
+  auto e = s->entries.find(it->second);
+  if (e == s->entries.end()) return VOX_REQ_UNKNOWN;
+  return e->second.state == Entry::RESIDENT ? VOX_REQ_RESIDENT : VOX_REQ_PENDING;
+}
+
+int vox_serve_poll(vox_serve* s, uint64_t id, int32_t* state) {
+  if (!s || !state) return VOX_ERR_INVALID;
+  const int st = poll_and_admit(s, false);
+  if (st != VOX_OK) return st;
+  *state = request_state(s, id);
+  return VOX_OK;
+}
+
+int vox_serve_wait(vox_serve* s, uint64_t id, double timeout_s) {
+  if (!s) return VOX_ERR_INVALID;
+  const double deadline = mono_now() + timeout_s;
+  for (;;) {
+    int st = poll_and_admit(s, false);
+    if (st != VOX_OK) return st;
+    const int32_t r = request_state(s, id);
+    if (r == VOX_REQ_RESIDENT) return VOX_OK;
+    if (r == VOX_REQ_UNKNOWN) return VOX_ERR_INVALID;
+    bool busy = false;
+    for (Slot& sl : s->slots) busy = busy || sl.busy;
+    if (!busy && !s->queue.empty()) return VOX_ERR_OOM;  // the budget cannot hold its batch
+    if (mono_now() >= deadline) return VOX_ERR_TIMEOUT;
+    std::this_thread::sleep_for(std::chrono::microseconds(20));
+  }
 }
 
 int vox_serve_drain(vox_serve* s) {

@@ -31,6 +31,7 @@ GEN_HEIGHTMAP, GEN_DENSITY, GEN_BERNOULLI = 0, 1, 2
 CULL_REFERENCE, CULL_FULL6 = 0, 1
 LAYOUT_VERTEX, LAYOUT_INSTANCED = 0, 1
 SCHEDULE_LOOKBACK, SCHEDULE_PHASED = 0, 1
+VOX_REQ_UNKNOWN, VOX_REQ_PENDING, VOX_REQ_RESIDENT = 0, 1, 2
 # TEXTURE_INDEX_LIST row of GRASS (src/texture.rs:240-243), by face slot L R Bk F Up Down.
 GRASS_TEXTURES = (0, 0, 0, 0, 2, 1)
 
@@ -138,12 +139,16 @@ _SIGS = {
     "vox_graph_capture": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, ctypes.c_int64, _P, _P,
                                          ctypes.c_uint64, _P, ctypes.POINTER(_P)]),
     "vox_graph_launch": (ctypes.c_int, [_P]),
+    "vox_draw_list": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int32, _P, _P]),
     "vox_graph_destroy": (ctypes.c_int, [_P]),
     "vox_serve_create": (ctypes.c_int, [ctypes.POINTER(ServeConfig), ctypes.POINTER(_P)]),
     "vox_serve_destroy": (ctypes.c_int, [_P]),
     "vox_serve_now": (ctypes.c_double, []),
     "vox_serve_frame": (ctypes.c_int, [_P, _P, _P, ctypes.c_double]),
     "vox_serve_drain": (ctypes.c_int, [_P]),
+    "vox_serve_submit": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_double, _P]),
+    "vox_serve_poll": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int32)]),
+    "vox_serve_wait": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_double]),
     "vox_serve_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(ServeStats)]),
     "vox_serve_lookup": (ctypes.c_int, [_P, ChunkCoord, ctypes.POINTER(_P), ctypes.POINTER(_P),
                                         ctypes.POINTER(ctypes.c_uint64)]),
@@ -337,6 +342,13 @@ class Context:
     def selftest_lookback_timeout(self, spin_limit: int) -> int:
         return self._lib.vox_selftest_lookback_timeout(self._h, spin_limit)
 
+    def draw_list(self, planes, d_coords, d_offsets, n: int, d_draws, d_count):
+        """vox_draw_list: indirect draw records of the visible chunks with faces."""
+        p = (ctypes.c_float * 24)(*[float(v) for v in planes])
+        self._check(self._lib.vox_draw_list(self._h, ctypes.addressof(p), _ptr(d_coords),
+                                            _ptr(d_offsets), n, _ptr(d_draws), _ptr(d_count)),
+                    "vox_draw_list")
+
     def capture_graph(self, d_coords, d_nbr_mask, n: int, d_out0, d_out1, cap_faces: int,
                       d_offsets, chunk_index_base: int = 0) -> "Graph":
         """vox_graph_capture: one fused batch launch captured as a CUDA graph."""
@@ -429,6 +441,28 @@ class Server:
         st = self._lib.vox_serve_drain(self._h)
         if st != VOX_OK:
             raise VoxError(st, "vox_serve_drain")
+
+    def submit(self, coords, now=-1.0):
+        """vox_serve_submit: request ids of the chunks (existing ids for known chunks)."""
+        import numpy as np
+        c = np.ascontiguousarray(np.asarray(coords, np.int32).reshape(-1, 3))
+        ids = np.zeros(len(c), np.uint64)
+        st = self._lib.vox_serve_submit(self._h, c.ctypes.data, len(c), now, ids.ctypes.data)
+        if st != VOX_OK:
+            raise VoxError(st, "vox_serve_submit")
+        return [int(v) for v in ids]
+
+    def poll(self, req_id) -> int:
+        """VOX_REQ_UNKNOWN, VOX_REQ_PENDING or VOX_REQ_RESIDENT."""
+        state = ctypes.c_int32()
+        st = self._lib.vox_serve_poll(self._h, req_id, ctypes.byref(state))
+        if st != VOX_OK:
+            raise VoxError(st, "vox_serve_poll")
+        return state.value
+
+    def wait(self, req_id, timeout_s=10.0) -> int:
+        """vox_serve_wait; returns the status (VOX_OK when resident)."""
+        return self._lib.vox_serve_wait(self._h, req_id, timeout_s)
 
     def stats(self) -> ServeStats:
         s = ServeStats()
