@@ -312,8 +312,11 @@ int issue_batch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out, cudaStream_t s
   if (ctx->schedule == VOX_SCHEDULE_PHASED) {
     const void* fn = ctx->ks->phased[gm][layout][ctx->topt];
     const int grid = std::max(1, std::min(a.n, host_out ? ctx->host_grid[gm] : ctx->phased_grid[gm]));
-    // emission items per chunk: one, unless there are fewer chunks than CTAs
-    a.split = std::max(1, std::min(8, grid / a.n));
+    // emission items per chunk: one for small chunks unless there are fewer chunks than
+    // CTAs; chunks of 32^3 and up (whose emission dwarfs an item's reload) split until
+    // there are about eight items per CTA, which evens out the last wave
+    a.split = ctx->cfg.chunk_size >= 32 ? std::max(1, std::min(8, (8 * grid + a.n - 1) / a.n))
+                                        : std::max(1, std::min(8, grid / a.n));
     VOX_CUDA(ctx, cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), params, (size_t)smem,
                                               stream),
              "cudaLaunchCooperativeKernel");

@@ -410,7 +410,9 @@ __device__ void gen_heightmap(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, 
       f = f * g.lac;
       amp = amp * g.gain;
     }
-    __syncthreads();
+    // the next group rewrites the lattice data; after the last group the thresholds
+    // below use only this thread's sums
+    if (o0 + kOctGroup < g.octaves) __syncthreads();
   }
 #pragma unroll
   for (int c = 0; c < CPT; ++c) {
@@ -795,7 +797,9 @@ __device__ uint32_t count_and_scan(ChunkSmem<N, LAYOUT>& s) {
   unsigned long long* wsum = reinterpret_cast<unsigned long long*>(s.stage);  // staging is free
   if (lane == 31) wsum[warp] = incl;
   __syncthreads();
-  if (warp == 0) {
+  // every warp scans the warp totals itself (no second barrier)
+  unsigned long long before = 0, tot = 0;
+  {
     const unsigned long long v = lane < nwarps ? wsum[lane] : 0ull;
     unsigned long long vi = v;
 #pragma unroll
@@ -803,12 +807,10 @@ __device__ uint32_t count_and_scan(ChunkSmem<N, LAYOUT>& s) {
       const unsigned long long u = __shfl_up_sync(0xffffffffu, vi, off);
       if (lane >= off) vi += u;
     }
-    if (lane < nwarps) wsum[32 + lane] = vi - v;  // exclusive warp offsets
-    if (lane == nwarps - 1) wsum[64] = vi;         // chunk totals
+    before = __shfl_sync(0xffffffffu, vi - v, warp);  // exclusive offset of this warp
+    tot = __shfl_sync(0xffffffffu, vi, nwarps - 1);   // chunk totals
   }
-  __syncthreads();
-  const unsigned long long excl = wsum[32 + warp] + incl - mine;
-  const unsigned long long tot = wsum[64];
+  const unsigned long long excl = before + incl - mine;
   const uint32_t nvox = (uint32_t)(tot >> 20) & 0xFFFFFu;
   const bool use_list = VCap > 0 && nvox <= (uint32_t)VCap;
   uint32_t run = (uint32_t)(excl >> 40);
