@@ -15,6 +15,7 @@
  *   Frustum::contains                   src/frustum_culling.rs:16-40 -> vox_frustum_cull
  *   World::render (draw loop)           src/world.rs:24-40        -> vox_draw_list
  *   ChunkGenerator per-tick dispatch    src/chunk_builder.rs:69-132 -> vox_graph_capture/launch
+ *   vertex.vert + pipeline (render)     src/renderer/pipeline.rs:36-45 -> vox_raster (headless)
  *
  * Conventions
  *  - Every call returns an int status (VOX_OK = 0, see vox_status).
@@ -260,6 +261,23 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
  * publishes. Returns VOX_ERR_TIMEOUT after spin_limit polls (no hang, no trap) and leaves
  * the context usable. */
 int vox_selftest_lookback_timeout(vox_ctx* ctx, int32_t spin_limit);
+
+/* ---- Headless rasteriser ---------------------------------------------------------------- */
+
+/* Renders vertex-layout faces (d_vertices: 96 B per face, d_indices: 6 u32 per face) into
+ * an RGBA8 image of width x height, for visual regression: gl_Position = view_proj *
+ * vertex (src/shaders/vertex.vert:22-27), counter-clockwise front faces with back faces
+ * culled and depth test Less against a clear depth of 1.0
+ * (src/renderer/pipeline.rs:36-45), clear colour (0.1, 0.2, 0.3)
+ * (src/renderer/renderer.rs:92-99), pixel centres at +0.5 with the top-left fill rule,
+ * perspective-correct texture coordinates. The texture images are replaced by a
+ * procedural palette per texture index with a 4x4 checker in (u, v). Triangles with a
+ * vertex behind the camera (clip w <= 0) are dropped (no near-plane clipping).
+ * d_depth_keys is width x height u64 of scratch. Requires the vertex layout and
+ * faces < 2^31. Equal inputs give equal bytes in any execution order. */
+int vox_raster(vox_ctx* ctx, const float view_proj_colmajor[16], const void* d_vertices,
+               const void* d_indices, uint64_t faces, int32_t width, int32_t height,
+               uint64_t* d_depth_keys, uint8_t* d_rgba);
 
 /* ---- CUDA graph replay of the fused batch ---------------------------------------------- */
 

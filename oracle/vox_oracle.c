@@ -802,3 +802,142 @@ int or_noise_error_stats(const vox_config* cfg, const vox_chunk_coord* coords, i
   free(v32);
   return VOX_OK;
 }
+
+/* ------------------------------------------------------------------------------------ */
+/* Headless rasteriser (project spec; vertex stage src/shaders/vertex.vert:22-27,        */
+/* pipeline state src/renderer/pipeline.rs:36-45, clear src/renderer/renderer.rs:92-105) */
+/* ------------------------------------------------------------------------------------ */
+
+typedef struct {
+  float x, y, z, w, u, v;
+} or_sv;
+
+static int or_to_screen(const float* m, const uint8_t* vertices, uint64_t g, int k, int W, int H,
+                        or_sv* o) {
+  float vx[5];
+  memcpy(vx, vertices + g * 96 + (uint64_t)k * 24, sizeof vx);
+  const float px = vx[0], py = vx[1], pz = vx[2];
+  const float cx = ((m[0] * px + m[4] * py) + m[8] * pz) + m[12];
+  const float cy = ((m[1] * px + m[5] * py) + m[9] * pz) + m[13];
+  const float cz = ((m[2] * px + m[6] * py) + m[10] * pz) + m[14];
+  const float cw = ((m[3] * px + m[7] * py) + m[11] * pz) + m[15];
+  if (!(cw > 0.0f)) return 0;
+  const float nx = cx / cw, ny = cy / cw, nz = cz / cw;
+  o->x = (nx + 1.0f) * 0.5f * (float)W;
+  o->y = (1.0f - ny) * 0.5f * (float)H;
+  o->z = nz;
+  o->w = cw;
+  o->u = vx[3];
+  o->v = vx[4];
+  return 1;
+}
+
+static float or_edge(const or_sv* a, const or_sv* b, float px, float py) {
+  return (b->x - a->x) * (py - a->y) - (b->y - a->y) * (px - a->x);
+}
+
+static int or_top_left(const or_sv* a, const or_sv* b) {
+  const float dx = b->x - a->x, dy = b->y - a->y;
+  return dy < 0.0f || (dy == 0.0f && dx > 0.0f);
+}
+
+static int or_tri_setup(const float* m, const uint8_t* vertices, const uint8_t* indices,
+                        uint64_t g, int t, int W, int H, or_sv* v0, or_sv* v1, or_sv* v2,
+                        float* area) {
+  uint32_t ix[3];
+  memcpy(ix, indices + g * 24 + (uint64_t)t * 12, sizeof ix);
+  if (!or_to_screen(m, vertices, g, (int)(ix[0] & 3u), W, H, v0) ||
+      !or_to_screen(m, vertices, g, (int)(ix[1] & 3u), W, H, v1) ||
+      !or_to_screen(m, vertices, g, (int)(ix[2] & 3u), W, H, v2))
+    return 0;
+  float a = or_edge(v0, v1, v2->x, v2->y);
+  if (!(a < 0.0f)) return 0; /* back face (clockwise in NDC) or degenerate */
+  const or_sv tmp = *v1;
+  *v1 = *v2;
+  *v2 = tmp;
+  *area = -a;
+  return 1;
+}
+
+static uint32_t or_float_bits(float f) {
+  uint32_t u;
+  memcpy(&u, &f, sizeof u);
+  return u;
+}
+
+static void or_shade(uint32_t tex, float u, float v, uint8_t* rgba) {
+  static const float pal[4][3] = {{0.45f, 0.55f, 0.25f}, {0.45f, 0.32f, 0.20f},
+                                  {0.30f, 0.70f, 0.25f}, {0.60f, 0.60f, 0.60f}};
+  const float* c = pal[tex & 3u];
+  const int cu = (int)floorf(u * 4.0f), cv = (int)floorf(v * 4.0f);
+  const float f = ((cu + cv) & 1) ? 0.85f : 1.0f;
+  for (int k = 0; k < 3; ++k) rgba[k] = (uint8_t)(c[k] * f * 255.0f + 0.5f);
+  rgba[3] = 255;
+}
+
+void or_raster(const float m[16], const void* vertices_, const void* indices_, uint64_t faces,
+               int W, int H, const uint32_t tex[6], uint8_t* rgba) {
+  const uint8_t* vertices = (const uint8_t*)vertices_;
+  const uint8_t* indices = (const uint8_t*)indices_;
+  const size_t npx = (size_t)W * (size_t)H;
+  uint64_t* keys = (uint64_t*)malloc(npx * sizeof(uint64_t));
+  if (!keys) return;
+  for (size_t i = 0; i < npx; ++i) keys[i] = ~0ull;
+  for (uint64_t tri = 0; tri < 2 * faces; ++tri) {
+    or_sv v0, v1, v2;
+    float area;
+    if (!or_tri_setup(m, vertices, indices, tri >> 1, (int)(tri & 1), W, H, &v0, &v1, &v2, &area))
+      continue;
+    const float fx0 = fminf(fminf(v0.x, v1.x), v2.x), fx1 = fmaxf(fmaxf(v0.x, v1.x), v2.x);
+    const float fy0 = fminf(fminf(v0.y, v1.y), v2.y), fy1 = fmaxf(fmaxf(v0.y, v1.y), v2.y);
+    if (fx1 < 0.0f || fy1 < 0.0f || fx0 > (float)W || fy0 > (float)H) continue;
+    int x0 = (int)floorf(fx0), x1 = (int)ceilf(fx1), y0 = (int)floorf(fy0), y1 = (int)ceilf(fy1);
+    if (x0 < 0) x0 = 0;
+    if (y0 < 0) y0 = 0;
+    if (x1 > W - 1) x1 = W - 1;
+    if (y1 > H - 1) y1 = H - 1;
+    const int tl0 = or_top_left(&v1, &v2), tl1 = or_top_left(&v2, &v0), tl2 = or_top_left(&v0, &v1);
+    for (int py = y0; py <= y1; ++py) {
+      const float sy = (float)py + 0.5f;
+      for (int px = x0; px <= x1; ++px) {
+        const float sx = (float)px + 0.5f;
+        const float w0 = or_edge(&v1, &v2, sx, sy), w1 = or_edge(&v2, &v0, sx, sy),
+                    w2 = or_edge(&v0, &v1, sx, sy);
+        const int in = (w0 > 0.0f || (w0 == 0.0f && tl0)) && (w1 > 0.0f || (w1 == 0.0f && tl1)) &&
+                       (w2 > 0.0f || (w2 == 0.0f && tl2));
+        if (!in) continue;
+        float z = ((w0 * v0.z + w1 * v1.z) + w2 * v2.z) / area;
+        if (!(z >= 0.0f && z < 1.0f)) continue;
+        z = z + 0.0f;
+        const uint64_t key = ((uint64_t)or_float_bits(z) << 32) | (uint64_t)(uint32_t)tri;
+        uint64_t* k = keys + (size_t)py * W + px;
+        if (key < *k) *k = key;
+      }
+    }
+  }
+  for (size_t i = 0; i < npx; ++i) {
+    uint8_t* o = rgba + 4 * i;
+    if (keys[i] == ~0ull) {
+      o[0] = (uint8_t)(0.1f * 255.0f + 0.5f);
+      o[1] = (uint8_t)(0.2f * 255.0f + 0.5f);
+      o[2] = (uint8_t)(0.3f * 255.0f + 0.5f);
+      o[3] = 255;
+      continue;
+    }
+    const uint64_t tri = keys[i] & 0xFFFFFFFFull, g = tri >> 1;
+    or_sv v0, v1, v2;
+    float area;
+    or_tri_setup(m, vertices, indices, g, (int)(tri & 1), W, H, &v0, &v1, &v2, &area);
+    const float sx = (float)(i % (size_t)W) + 0.5f, sy = (float)(i / (size_t)W) + 0.5f;
+    const float w0 = or_edge(&v1, &v2, sx, sy), w1 = or_edge(&v2, &v0, sx, sy),
+                w2 = or_edge(&v0, &v1, sx, sy);
+    const float b0 = w0 / v0.w, b1 = w1 / v1.w, b2 = w2 / v2.w;
+    const float den = (b0 + b1) + b2;
+    const float u = ((b0 * v0.u + b1 * v1.u) + b2 * v2.u) / den;
+    const float v = ((b0 * v0.v + b1 * v1.v) + b2 * v2.v) / den;
+    uint32_t slot;
+    memcpy(&slot, vertices + g * 96 + 20, sizeof slot);
+    or_shade(tex[slot < 6u ? slot : 0u], u, v, o);
+  }
+  free(keys);
+}

@@ -107,6 +107,15 @@ int64_t or_baseline_run(const vox_config* cfg, const vox_chunk_coord* coords,
 void or_frustum_planes(const float m_colmajor[16], float planes[24]);
 int or_frustum_contains(const float planes[24], vox_chunk_coord coord, int chunk_extent);
 
+/* Headless rasteriser (the GPU's vox_raster restated, for visual regression images):
+ * vertex-layout faces through the global matrix (src/shaders/vertex.vert:22-27), back faces
+ * culled with counter-clockwise fronts, depth Less against 1.0
+ * (src/renderer/pipeline.rs:36-45), clear colour (0.1, 0.2, 0.3)
+ * (src/renderer/renderer.rs:92-99), top-left fill rule at pixel centres, perspective-correct
+ * (u, v) and a procedural palette per texture index. Writes width x height RGBA8. */
+void or_raster(const float m_colmajor[16], const void* vertices, const void* indices,
+               uint64_t faces, int width, int height, const uint32_t tex[6], uint8_t* rgba);
+
 /* Noise precision report: FP32 generator values against FP64 at every voxel of the
  * chunks (density: d; heightmap: the column heights). max_abs_err = max |f32 - f64|;
  * near_threshold = voxels whose FP64 value lies within max_abs_err of the solid/air

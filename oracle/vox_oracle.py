@@ -57,6 +57,7 @@ def load() -> ctypes.CDLL:
                                              ctypes.c_int]),
         "or_frustum_planes": (None, [_P, _P]),
         "or_frustum_contains": (ctypes.c_int, [_P, _Coord, ctypes.c_int]),
+        "or_raster": (None, [_P, _P, _P, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, _P, _P]),
         "or_noise_error_stats": (ctypes.c_int, [_P, _P, ctypes.c_int32,
                                                 ctypes.POINTER(ctypes.c_double),
                                                 ctypes.POINTER(ctypes.c_int64),
@@ -191,6 +192,17 @@ def frustum_planes(m_colmajor) -> np.ndarray:
 def frustum_contains(planes, coord, extent: int) -> bool:
     p = np.ascontiguousarray(np.asarray(planes, np.float32).reshape(24))
     return bool(load().or_frustum_contains(_addr(p), _Coord(*coord), extent))
+
+
+def raster(view_proj, vertices, indices, faces: int, width: int, height: int, tex) -> np.ndarray:
+    """or_raster: RGBA8 image (height, width, 4) of vertex-layout faces."""
+    m = np.ascontiguousarray(np.asarray(view_proj, np.float32).reshape(16))
+    v = np.ascontiguousarray(np.frombuffer(bytes(vertices), np.uint8))
+    i = np.ascontiguousarray(np.frombuffer(bytes(indices), np.uint8))
+    t = np.ascontiguousarray(np.asarray(tex, np.uint32).reshape(6))
+    out = np.zeros((height, width, 4), np.uint8)
+    load().or_raster(_addr(m), _addr(v), _addr(i), faces, width, height, _addr(t), _addr(out))
+    return out
 
 
 def noise_error_stats(cfg, coords):

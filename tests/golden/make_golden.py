@@ -57,9 +57,42 @@ def digest(cfg, coords, masks, base):
     }
 
 
+# Camera views of the plain workload (Camera::update_global_matrix) for the rasteriser.
+RASTER_VIEWS = [((60.0, 45.0, 70.0), (-0.6, -0.45, -0.65)), ((0.5, 20.0, 0.5), (0.3, -0.25, 1.0))]
+RASTER_SIZE = (320, 180)
+
+
+def raster_images():
+    """The oracle's renders of the plain workload's mesh from RASTER_VIEWS."""
+    wl = voxgpu.workload("plain")
+    cfg = wl.config()
+    o0, o1, offs = vox_oracle.gen_mesh_batch(cfg, wl.coords, wl.masks())
+    W, H = RASTER_SIZE
+    return [vox_oracle.raster(voxgpu.camera_matrix(eye, d, zfar=400.0), o0, o1, int(offs[-1]), W, H,
+                              cfg.texture_index) for eye, d in RASTER_VIEWS]
+
+
+def write_png(path, img):
+    """A minimal RGB PNG (stored scanlines, zlib) for looking at a render."""
+    import struct
+    import zlib
+    h, w = img.shape[:2]
+    raw = b"".join(b"\x00" + img[y, :, :3].tobytes() for y in range(h))
+
+    def chunk(t, d):
+        return struct.pack(">I", len(d)) + t + d + struct.pack(">I", zlib.crc32(t + d) & 0xFFFFFFFF)
+    with open(path, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0))
+                + chunk(b"IDAT", zlib.compress(raw, 9)) + chunk(b"IEND", b""))
+
+
 def main():
     data = {name: digest(cfg, coords, masks, base) for name, cfg, coords, masks, base in cases()}
     data["perm42_first16"] = vox_oracle.perm(42)[:16].tolist()
+    imgs = raster_images()
+    data["raster_plain_sha256"] = [hashlib.sha256(im.tobytes()).hexdigest() for im in imgs]
+    for k, im in enumerate(imgs):
+        write_png(os.path.join(HERE, f"raster_plain_view{k}.png"), im)
     with open(os.path.join(HERE, "oracle_digests.json"), "w") as f:
         json.dump(data, f, indent=1, sort_keys=True)
         f.write("\n")

@@ -19,6 +19,18 @@ def test_oracle_matches_golden_digests(oracle):
     assert oracle.perm(42)[:16].tolist() == want["perm42_first16"]
 
 
+def test_oracle_raster_matches_golden_images(oracle):
+    """The oracle's renders of the plain workload (tests/golden/raster_plain_view*.png are
+    the same images, for viewing) against their committed digests."""
+    import hashlib
+    import sys
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    import make_golden
+    want = json.load(open(os.path.join(HERE, "golden", "oracle_digests.json")))
+    got = [hashlib.sha256(im.tobytes()).hexdigest() for im in make_golden.raster_images()]
+    assert got == want["raster_plain_sha256"]
+
+
 @pytest.mark.parametrize("name,max_err,max_mismatch", [("plain", 1e-5, 4), ("heightmap", 5e-5, 4)])
 def test_fp32_noise_error_against_fp64(vox, oracle, name, max_err, max_mismatch):
     wl = vox.workload(name)

@@ -3,6 +3,8 @@
 Occupancy, face counts, offsets and every byte of the emitted vertex / index /
 instance records must equal the oracle's on the same inputs (signed zeros included).
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -409,14 +411,12 @@ def test_frustum_matches_oracle(vox, oracle):
 def test_draw_list_matches_oracle(vox, oracle, layout):
     """World::render as an indirect draw list: the visible chunks with faces, in chunk
     order, with the vertex / instance ranges of their meshes."""
-    from test_oracle_kat import perspective_look
     wl = vox.workload("heightmap")
     cfg = wl.config(layout=layout)
     coords = list(wl.coords[:600])
     masks = vox.neighbour_masks(coords)
     _, _, offs = oracle.gen_mesh_batch(cfg, coords, masks)
-    eye = (100.0, 40.0, 60.0)
-    m = perspective_look(eye, (1.0, -0.3, 0.4))
+    m = vox.camera_matrix((100.0, 40.0, 60.0), (-1.0, -0.3, -0.4), zfar=300.0)
     planes = oracle.frustum_planes(m)
     want = []
     for i, c in enumerate(coords):
@@ -561,4 +561,33 @@ def test_single_chunk_direct_and_staged(vox, oracle, stage):
     ctx.sync()
     assert int(to_np(cnt)[0]) == wc
     assert np.array_equal(to_np(o0, wc * 96), w0) and np.array_equal(to_np(o1, wc * 24), w1)
+    ctx.close()
+
+
+@pytest.mark.parametrize("view", [0, 1])
+def test_raster_matches_oracle(vox, oracle, view):
+    """The headless rasteriser renders the plain workload's mesh byte for byte like the
+    oracle's rasteriser (order-independent depth resolution)."""
+    wl = vox.workload("plain")
+    cfg = wl.config()
+    w0, w1, woffs = oracle.gen_mesh_batch(cfg, wl.coords, wl.masks())
+    faces = int(woffs[-1])
+    eye, d = [((60.0, 45.0, 70.0), (-0.6, -0.45, -0.65)), ((0.5, 20.0, 0.5), (0.3, -0.25, 1.0))][view]
+    m = vox.camera_matrix(eye, d, zfar=400.0)  # Camera::update_global_matrix, column-major
+    W, H = 320, 180
+    want = oracle.raster(m, w0, w1, faces, W, H, cfg.texture_index)
+    bg = (want.reshape(-1, 4) == np.array([26, 51, 77, 255], np.uint8)).all(1).mean()
+    assert 0.2 < bg < 0.9 and len(np.unique(want.reshape(-1, 4), axis=0)) >= 5
+    ctx = ctx_for(vox, cfg)
+    d0, d1 = to_dev(np.frombuffer(w0, np.uint8)), to_dev(np.frombuffer(w1, np.uint8))
+    keys = dev_bytes(W * H * 8)
+    rgba = dev_bytes(W * H * 4)
+    lib = vox.lib()
+    mm = (ctypes.c_float * 16)(*[float(v) for v in np.asarray(m, np.float32).reshape(16)])
+    st = lib.vox_raster(ctx._h, ctypes.addressof(mm), d0.data_ptr(), d1.data_ptr(), faces, W, H,
+                        keys.data_ptr(), rgba.data_ptr())
+    assert st == vox.VOX_OK
+    ctx.sync()
+    got = to_np(rgba, W * H * 4).reshape(H, W, 4)
+    assert np.array_equal(got, want)
     ctx.close()

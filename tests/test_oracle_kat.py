@@ -199,3 +199,50 @@ def test_frustum(oracle):
     # frustum_culling.rs:27-39 tests only the 8 corners: the chunk around the eye has no
     # corner inside the view volume and is reported invisible (a reference quirk).
     assert not oracle.frustum_contains(planes, (0, 0, 0), 32)
+
+
+def _one_face(slot, order=(0, 2, 1, 3, 1, 2), z=0.5):
+    """One vertex-layout face: quad::VERTICES at depth z (NDC), texture slot `slot`."""
+    pos = [(-0.5, 0.5), (0.5, 0.5), (-0.5, -0.5), (0.5, -0.5)]
+    uv = [(0.0, 0.0), (1.0, 0.0), (0.0, 1.0), (1.0, 1.0)]
+    v = b"".join(np.array([p[0], p[1], z, t[0], t[1]], np.float32).tobytes()
+                 + np.array([slot], np.uint32).tobytes() for p, t in zip(pos, uv))
+    return v, np.array(order, np.uint32).tobytes()
+
+
+def test_raster_single_face_known_pixels(oracle):
+    """Identity matrix, one front face covering NDC [-0.5, 0.5]^2 on an 8x8 image: pixels
+    2..5 in x and y carry the checkered top colour, everything else the clear colour."""
+    ident = np.eye(4, dtype=np.float32).reshape(16)
+    tex = (0, 0, 0, 0, 2, 1)
+    v, i = _one_face(4)
+    img = oracle.raster(ident, v, i, 1, 8, 8, tex)
+    clear = (26, 51, 77, 255)
+    light, dark = (77, 179, 64, 255), (65, 152, 54, 255)
+    for py in range(8):
+        for px in range(8):
+            got = tuple(int(c) for c in img[py, px])
+            if 2 <= px <= 5 and 2 <= py <= 5:
+                want = light if ((px - 2) + (py - 2)) % 2 == 0 else dark
+            else:
+                want = clear
+            assert got == want, (px, py, got, want)
+    # the same face wound the other way is a back face: culled
+    vb, ib = _one_face(4, order=(0, 1, 2, 3, 2, 1))
+    img = oracle.raster(ident, vb, ib, 1, 8, 8, tex)
+    assert (img.reshape(-1, 4) == np.array(clear, np.uint8)).all()
+
+
+def test_raster_depth_less_first_drawn_wins(oracle):
+    """Two faces at the same depth: the first drawn keeps the pixels (depth test Less);
+    a nearer face drawn later replaces them."""
+    ident = np.eye(4, dtype=np.float32).reshape(16)
+    tex = (0, 0, 0, 0, 2, 1)
+    v_top, i_top = _one_face(4, z=0.5)
+    v_side, _ = _one_face(0, z=0.5)
+    i2 = np.array([0, 2, 1, 3, 1, 2, 4, 6, 5, 7, 5, 6], np.uint32).tobytes()
+    img = oracle.raster(ident, v_top + v_side, i2, 2, 8, 8, tex)
+    assert tuple(int(c) for c in img[2, 2]) == (77, 179, 64, 255)   # top colour (first)
+    v_near, _ = _one_face(0, z=0.25)
+    img = oracle.raster(ident, v_top + v_near, i2, 2, 8, 8, tex)
+    assert tuple(int(c) for c in img[2, 2]) == (115, 140, 64, 255)  # side colour (nearer)

@@ -791,6 +791,30 @@ int vox_draw_list(vox_ctx* ctx, const float planes[24], const vox_chunk_coord* d
   return VOX_OK;
 }
 
+int vox_raster(vox_ctx* ctx, const float view_proj_colmajor[16], const void* d_vertices,
+               const void* d_indices, uint64_t faces, int32_t width, int32_t height,
+               uint64_t* d_depth_keys, uint8_t* d_rgba) {
+  if (!ctx) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (ctx->cfg.layout != VOX_LAYOUT_VERTEX)
+    return fail(ctx, VOX_ERR_INVALID, "the rasteriser takes the vertex layout");
+  if (!view_proj_colmajor || width <= 0 || height <= 0 || width > 16384 || height > 16384 ||
+      !d_depth_keys || !d_rgba || faces >= (1ull << 31) || (faces > 0 && (!d_vertices || !d_indices)))
+    return fail(ctx, VOX_ERR_INVALID, "bad arguments");
+  RasterArgs a;
+  a.vertices = d_vertices;
+  a.indices = d_indices;
+  a.faces = faces;
+  a.width = width;
+  a.height = height;
+  std::memcpy(a.m, view_proj_colmajor, sizeof a.m);
+  std::memcpy(a.tex, ctx->cfg.texture_index, sizeof a.tex);
+  VOX_CUDA(ctx, launch_raster(a, reinterpret_cast<unsigned long long*>(d_depth_keys), d_rgba,
+                              ctx->stream),
+           "raster");
+  return VOX_OK;
+}
+
 int vox_ctx_get_tuning(vox_ctx* ctx, vox_tuning* out) {
   if (!ctx || !out) return VOX_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->mu);

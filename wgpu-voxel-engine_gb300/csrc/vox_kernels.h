@@ -36,6 +36,17 @@ struct Planes {
 cudaError_t launch_frustum(const Planes& planes, const void* coords, int n, int extent,
                            uint8_t* visible, cudaStream_t st);
 using DrawRecord = vox_draw_indexed_indirect;
+struct RasterArgs {
+  const void* vertices;     // vertex-layout records, 96 B per face
+  const void* indices;      // 6 u32 per face
+  unsigned long long faces;
+  int width, height;
+  float m[16];              // global matrix, column-major
+  uint32_t tex[6];          // texture index per face slot
+};
+// Renders the faces into rgba (width x height x 4 bytes); keys: width x height u64.
+cudaError_t launch_raster(const RasterArgs& a, unsigned long long* keys, uint8_t* rgba,
+                          cudaStream_t st);
 cudaError_t launch_draw_list(const Planes& planes, const void* coords,
                              const unsigned long long* offs, int n, int extent, int instanced,
                              DrawRecord* out, uint32_t* count, unsigned* err, cudaStream_t st);

@@ -131,6 +131,8 @@ _SIGS = {
                                                   ctypes.c_uint64, _P]),
     "vox_frustum_planes": (ctypes.c_int, [_P, _P]),
     "vox_frustum_cull": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, _P]),
+    "vox_raster": (ctypes.c_int, [_P, _P, _P, _P, ctypes.c_uint64, ctypes.c_int32, ctypes.c_int32,
+                                  _P, _P]),
     "vox_ctx_get_tuning": (ctypes.c_int, [_P, ctypes.POINTER(Tuning)]),
     "vox_ctx_set_tuning": (ctypes.c_int, [_P, ctypes.POINTER(Tuning)]),
     "vox_autotune": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, ctypes.c_int64, _P, _P,
