@@ -73,8 +73,9 @@ template <int N>
 __host__ __device__ constexpr int dens_scratch_bytes() {
   return 64 + kDensMaxOct * 3 * (N + 2) * 16 + dens_max_corners<N>() * 16;
 }
-// Faces one warp's 32 voxels can have (6 each): the size of a warp's face list.
-constexpr int kWarpFaces = 32 * 6;
+// A warp's face list: the faces of one group of 32 voxels (6 each) after fewer than one
+// batch of faces carried over from the previous group.
+constexpr int kWarpFaces = 32 * 6 + 32;
 // Faces one warp stages at a time (each warp has two staging buffers of this many faces).
 constexpr int kWarpBatch = 32;
 // Bytes of one warp staging buffer (vertex records, then the index records shifted by up
@@ -1175,22 +1176,53 @@ __device__ __forceinline__ void warp_send_faces(const TablesDev* tab, const uint
   }
 }
 
+// Emission of elements [lo, hi): warp w takes the contiguous run [lo + w*per, ...) of
+// whole groups of 32 elements, so consecutive groups' faces are adjacent in the output.
+// Faces accumulate in the warp's list and leave in full batches of 32 (the send step);
+// fewer than 32 are carried to the next group, and the rest leave at the end.
+template <int N, int LAYOUT, typename Send>
+__device__ __forceinline__ void emit_runs(ChunkSmem<N, LAYOUT>& s, int lo, int hi, Send send) {
+  const bool use_list = s.misc[1] >= 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  uint32_t* list = s.lists + warp * kWarpFaces;
+  const int groups = (hi - lo + 31) >> 5;
+  const int gper = (groups + nwarps - 1) / nwarps;
+  const int wlo = lo + warp * gper * 32;
+  const int whi = min(hi, wlo + gper * 32);
+  int have = 0;             // faces waiting in list[0, have)
+  uint32_t first_have = 0;  // chunk-local index of list[0]
+  for (int base = wlo; base < whi; base += 32) {
+    uint32_t first;
+    const int nwf = warp_faces<N, LAYOUT>(s, use_list, whi, base, list + have, first);
+    if (have == 0) first_have = first;
+    have += nwf;
+    const int full = have & ~31;
+    if (full > 0) {
+      send(list, full, first_have);
+      // move the remainder (< 32 faces) to the front of the list
+      const uint32_t keep = lane < have - full ? list[full + lane] : 0u;
+      __syncwarp();
+      if (lane < have - full) list[lane] = keep;
+      __syncwarp();
+      first_have += (uint32_t)full;
+      have -= full;
+    }
+  }
+  if (have > 0) send(list, have, first_have);
+}
+
 template <int N, int LAYOUT>
 __device__ void emit_chunk(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c, unsigned long long g0,
                            unsigned long long cap, void* out0, void* out1, int nbuf,
                            bool lane_flush, int lo, int hi) {
   constexpr int kBuf = warp_buf_bytes<LAYOUT>();
-  const bool use_list = s.misc[1] >= 0;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  uint32_t* list = s.lists + warp * kWarpFaces;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned char* bufs = s.stage + (size_t)warp * nbuf * kBuf;
   int b = 0;
-  for (int base = lo + warp * 32; base < hi; base += nwarps * 32) {
-    uint32_t first;
-    const int nwf = warp_faces<N, LAYOUT>(s, use_list, hi, base, list, first);
-    warp_send_faces<N, LAYOUT>(s.tab, list, nwf, first, c, g0, cap, out0, out1, bufs, nbuf,
+  emit_runs<N, LAYOUT>(s, lo, hi, [&](const uint32_t* list, int nf, uint32_t first) {
+    warp_send_faces<N, LAYOUT>(s.tab, list, nf, first, c, g0, cap, out0, out1, bufs, nbuf,
                                lane_flush, b);
-  }
+  });
   if (lane == 0) bulk_wait_read_all();
   __syncwarp();
 }
@@ -1261,14 +1293,9 @@ template <int N, int LAYOUT>
 __device__ void emit_chunk_direct(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c,
                                   unsigned long long g0, unsigned long long cap, void* out0,
                                   void* out1, int lo, int hi) {
-  const bool use_list = s.misc[1] >= 0;
-  const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  uint32_t* list = s.lists + warp * kWarpFaces;
-  for (int base = lo + warp * 32; base < hi; base += nwarps * 32) {
-    uint32_t first;
-    const int nwf = warp_faces<N, LAYOUT>(s, use_list, hi, base, list, first);
-    warp_store_faces<N, LAYOUT>(s.tab, list, nwf, first, c, g0, cap, out0, out1);
-  }
+  emit_runs<N, LAYOUT>(s, lo, hi, [&](const uint32_t* list, int nf, uint32_t first) {
+    warp_store_faces<N, LAYOUT>(s.tab, list, nf, first, c, g0, cap, out0, out1);
+  });
 }
 
 // ------------------------------------------------------------------------------------
