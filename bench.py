@@ -374,11 +374,17 @@ def run_ours(args):
     if rank == 0 and args.plain_steps > 0:
         plain = plain_per_chunk(ctx, wl, cfg, d_coords, stream, args, b0, b1, torch, np)
 
+    # the rebuild path: meshing from resident occupancy (workloads with neighbours)
+    rebuild = None
+    if rank == 0 and len(slabs) == 1 and not wl.isolated:
+        rebuild = mesh_from_occupancy(ctx, wl, cfg, d_coords, n_all, o0, o1, cap, total_faces,
+                                      stream, flush, args, torch, np)
     # end to end through the host-pointer entry point (pinned buffers); the stress output
     # (49 GB per 1024 chunks) is sampled on its first 64 chunks
     e2e = None
     if rank == 0:
-        n_e2e = min(n_all, 64) if args.workload == "stress" else n_all
+        # (within the first slab, whose offsets start at d_offs[0])
+        n_e2e = min(slabs[0][1], 64) if args.workload == "stress" else n_all
         faces_e2e = total_faces if n_e2e == n_all and len(slabs) == 1 else int(d_offs[n_e2e].item())
         e2e = e2e_host(ctx, wl, masks, n_e2e, faces_e2e, b0, b1, args, np)
         if n_e2e < n_all:
@@ -418,6 +424,8 @@ def run_ours(args):
         line["batched_vs_plain"] = value / world / plain["value"]
     if e2e:
         line["e2e"] = e2e
+    if rebuild:
+        line["mesh_from_occupancy"] = rebuild
     if rank == 0 and world == 1 and args.latency_frames > 0 and args.workload == "heightmap":
         # p50/p99 request-to-mesh latency of the streaming engine at the serving request
         # rate (real-time 60 frames/s camera), next to the batch throughput above
@@ -483,6 +491,42 @@ def plain_per_chunk(ctx, wl, cfg, d_coords, stream, args, b0, b1, torch, np):
     ms = t0.elapsed_time(t1) / args.plain_steps
     return {"value": k / (ms / 1e3), "unit": "chunks/s", "chunks_per_pass": k,
             "launches_per_chunk": 2, "ms_per_pass": ms}
+
+
+def mesh_from_occupancy(ctx, wl, cfg, d_coords, n, o0, o1, cap, total_faces, stream, flush, args,
+                        torch, np):
+    """The rebuild path (ChunkGenerator::process_rebuild_queue, src/chunk_builder.rs:89-112):
+    vox_mesh_batch over occupancy already resident in a device pool (filled once by
+    vox_generate, untimed), with the lateral neighbours' slots as the halo source."""
+    words = ctx.sizes.occ_words_per_chunk
+    pool = torch.empty(n * words, dtype=torch.int32, device="cuda")
+    index = {tuple(c): i for i, c in enumerate(wl.coords)}
+    nbr = np.full((n, 6), -1, np.int32)
+    for i, (x, y, z) in enumerate(wl.coords):
+        for d, (dx, dz) in enumerate(((-1, 0), (1, 0), (0, -1), (0, 1))):
+            nbr[i, d] = index.get((x + dx, y, z + dz), -1)
+    d_slots = torch.arange(n, dtype=torch.int32, device="cuda")
+    d_nbr = torch.from_numpy(nbr).cuda()
+    offs = torch.zeros(n + 1, dtype=torch.int64, device="cuda")
+    steps = max(3, args.steps // 4)
+    torch.cuda.synchronize()  # the buffers above were filled on the default stream
+    with torch.cuda.stream(stream):
+        ctx.generate(d_coords, n, pool, chunk_index_base=wl.index_base)
+        for _ in range(3):
+            ctx.mesh_batch(pool, n, d_slots, d_nbr, d_coords, n, o0, o1, cap, offs)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        for k in range(steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            ctx.mesh_batch(pool, n, d_slots, d_nbr, d_coords, n, o0, o1, cap, offs)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    assert ctx.sync(raise_on_error=False) == 0
+    assert int(offs[-1].item()) == total_faces, "the rebuild path must emit the same faces"
+    ms = statistics.median(a.elapsed_time(b) for a, b in ev)
+    return {"value": n / (ms / 1e3), "unit": "chunks/s", "ms_per_step": ms, "steps": steps,
+            "api": "vox_mesh_batch from device-resident occupancy (L2 flushed before each step)"}
 
 
 def e2e_host(ctx, wl, masks, n, total_faces, b0, b1, args, np):
