@@ -73,3 +73,38 @@ def test_no_cpu_fallback_without_gpu(vox):
     with pytest.raises(vox.VoxError) as e:
         vox.Context(vox.make_config())
     assert e.value.status in (vox.VOX_ERR_NO_DEVICE, vox.VOX_ERR_CUDA)
+
+
+def test_struct_layouts_match_the_c_headers(vox, tmp_path):
+    """sizeof / offsetof from the C compiler (the public headers) against the ctypes mirrors
+    and the documented record sizes."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    src = tmp_path / "layout.c"
+    src.write_text("""
+#include <stddef.h>
+#include <stdio.h>
+#include "voxgpu.h"
+#include "voxgpu_serve.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n",
+         sizeof(vox_chunk_coord), sizeof(vox_generator), sizeof(vox_config),
+         offsetof(vox_config, gen), sizeof(vox_vertex), sizeof(vox_instance_raw),
+         sizeof(vox_sizes), sizeof(vox_tuning), sizeof(vox_draw_indexed_indirect),
+         sizeof(vox_serve_config), sizeof(vox_serve_stats), offsetof(vox_serve_config, view_radius));
+  return 0;
+}
+""")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c99", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True,
+                                          check=True).stdout.split()]
+    want = [ctypes.sizeof(vox.ChunkCoord), ctypes.sizeof(vox.Generator), ctypes.sizeof(vox.Config),
+            vox.Config.gen.offset, 24, 68, ctypes.sizeof(vox.Sizes), ctypes.sizeof(vox.Tuning), 20,
+            ctypes.sizeof(vox.ServeConfig), ctypes.sizeof(vox.ServeStats),
+            vox.ServeConfig.view_radius.offset]
+    assert got == want
