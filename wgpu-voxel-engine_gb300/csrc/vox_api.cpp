@@ -317,6 +317,7 @@ int issue_batch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out, cudaStream_t s
     // there are about eight items per CTA, which evens out the last wave
     a.split = ctx->cfg.chunk_size >= 32 ? std::max(1, std::min(8, (8 * grid + a.n - 1) / a.n))
                                         : std::max(1, std::min(8, grid / a.n));
+    a.split = std::max(1, std::min(a.split, 0x7FFFFFFF / a.n));  // items = n * split fit an int
     VOX_CUDA(ctx, cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), params, (size_t)smem,
                                               stream),
              "cudaLaunchCooperativeKernel");
