@@ -50,6 +50,7 @@ struct vox_ctx {
   uint32_t* d_counts = nullptr;
   size_t scratch_cap = 0;  // chunks
   TablesDev* d_tables = nullptr;
+  TablesDev h_tables{};  // the fused batch kernels take the tables as a kernel parameter
   BatchCtl* d_ctl = nullptr;
   BatchCtl* h_ctl = nullptr;  // pinned
   unsigned long long* d_state = nullptr;
@@ -308,7 +309,7 @@ int issue_batch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out, cudaStream_t s
     a.stage_faces = kStageSingle;
     a.lane_flush = 1;
   }
-  void* params[] = {&a};
+  void* params[] = {&a, &ctx->h_tables};
   if (ctx->schedule == VOX_SCHEDULE_PHASED) {
     const void* fn = ctx->ks->phased[gm][layout][ctx->topt];
     const int grid = std::max(1, std::min(a.n, host_out ? ctx->host_grid[gm] : ctx->phased_grid[gm]));
@@ -428,6 +429,7 @@ int vox_ctx_create(const vox_config* cfg, void* stream, vox_ctx** out) {
   }
   TablesDev tab;
   build_tables(*cfg, tab);
+  ctx->h_tables = tab;
   if (cudaMalloc(&ctx->d_tables, sizeof(TablesDev)) != cudaSuccess) return cleanup(VOX_ERR_OOM);
   if (cudaMemcpy(ctx->d_tables, &tab, sizeof tab, cudaMemcpyHostToDevice) != cudaSuccess)
     return cleanup(VOX_ERR_CUDA);

@@ -1339,11 +1339,11 @@ __device__ __forceinline__ void prepare_chunk(ChunkSmem<N, LAYOUT>& s, const Mes
 
 template <int N, int GM, int LAYOUT, int T>
 __global__ void __launch_bounds__(T)
-k_mesh_batch(MeshArgs a) {
+k_mesh_batch(const __grid_constant__ MeshArgs a, const __grid_constant__ TablesDev tab) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ChunkSmem<N, LAYOUT> s;
   s.carve(smem_raw);
-  load_tables<N, LAYOUT>(s, a.tables);
+  load_tables<N, LAYOUT>(s, &tab);  // the tables travel as a kernel parameter
   __shared__ int s_item;
   __shared__ unsigned long long s_base;
   __shared__ unsigned s_epoch;
@@ -1498,7 +1498,7 @@ __device__ unsigned long long scan_counts(const uint32_t* counts, int n,
 
 template <int N, int GM, int LAYOUT, int T>
 __global__ void __launch_bounds__(T)
-k_mesh_batch_phased(MeshArgs a) {
+k_mesh_batch_phased(const __grid_constant__ MeshArgs a, const __grid_constant__ TablesDev tab) {
   using P = SmemPlan<N, LAYOUT>;
   // spill slot of a chunk: [occ | halo | rows] [nz] [vlist] [misc], laid out as in shared
   // memory; the lists are copied only as far as they are used
@@ -1510,7 +1510,7 @@ k_mesh_batch_phased(MeshArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ChunkSmem<N, LAYOUT> s;
   s.carve(smem_raw);
-  load_tables<N, LAYOUT>(s, a.tables);
+  load_tables<N, LAYOUT>(s, &tab);  // the tables travel as a kernel parameter
   __shared__ int s_item;
   __shared__ unsigned s_gen;
   __shared__ unsigned long long s_base;
