@@ -158,12 +158,11 @@ int gen_mode_of(int kind) {
   }
 }
 
-// Emission mode of the default tuning (before autotuning): direct global stores.
-int default_stage_faces(const KernelSet& ks, int layout) {
-  (void)ks;
-  (void)layout;
-  return 0;
-}
+// The default tuning (before any autotuning), the shape that measured fastest on the
+// heightmap, density and stress batches: the phased schedule with one staging buffer per
+// warp, and the larger CTA size for chunks up to 32^3.
+constexpr int kDefaultSchedule = VOX_SCHEDULE_PHASED;
+int default_topt(int chunk_size) { return chunk_size <= 32 ? 1 : 0; }
 
 // Allows `fn` up to `smem` bytes of dynamic shared memory (capped at what the device
 // grants one block beyond the kernel's static shared memory).
@@ -450,9 +449,10 @@ int vox_ctx_create(const vox_config* cfg, void* stream, vox_ctx** out) {
   const int gsmem = ctx->ks->smem_total(VOX_LAYOUT_VERTEX, ctx->ks->gen_threads, 0);
   for (int gm = 1; gm < 4; ++gm)
     if ((st = prepare_kernel(ctx, ctx->ks->generate[gm], gsmem)) != VOX_OK) return cleanup(st);
-  if ((st = apply_tuning(ctx, 0, default_stage_faces(*ctx->ks, layout), 0,
-                          VOX_SCHEDULE_LOOKBACK)) != VOX_OK)
+  if (apply_tuning(ctx, default_topt(cfg->chunk_size), kStageSingle, 0, kDefaultSchedule) != VOX_OK &&
+      (st = apply_tuning(ctx, 0, 0, 0, kDefaultSchedule)) != VOX_OK)  // no room to stage
     return cleanup(st);
+  ctx->last_error.clear();
   if ((st = ensure_state(ctx, 1024)) != VOX_OK) return cleanup(st);
   if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return cleanup(VOX_ERR_CUDA);
   *out = ctx;
