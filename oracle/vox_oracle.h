@@ -2,8 +2,8 @@
  * vox_oracle.h — CPU oracle for the chunk generation / meshing / frustum path.
  *
  * TEST INFRASTRUCTURE ONLY. This is a plain-C restatement of the reference's CPU
- * algorithm (Blatko1/wgpu-voxel-engine, Rust) used as the checker for the CUDA path
- * and, timed on the host cores, as the CPU baseline. Nothing in the product links,
+ * algorithm (Blatko1/wgpu-voxel-engine, Rust) that the CUDA path's outputs are compared
+ * against in the tests and, timed on the host cores, the CPU baseline. Nothing in the product links,
  * loads or calls it: only tests/, __graft_entry__.smoke() and bench.py's CPU legs do.
  *
  * Parity status: UNPINNED. The reference ships no tests, golden vectors or fixtures,

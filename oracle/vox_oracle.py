@@ -1,7 +1,8 @@
 """ctypes wrapper of the CPU oracle (liboracle_vox.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's
-CPU-baseline legs as the checker. Parity status: unpinned (see vox_oracle.h).
+CPU-baseline legs, to compare the CUDA path's outputs with. Parity status: unpinned (see
+vox_oracle.h).
 """
 from __future__ import annotations
 
