@@ -3,11 +3,13 @@
 // One CTA owns one chunk at a time. The chunk's occupancy lives in shared memory as
 // one N-bit row per (y, z) (bit x = voxel solid), plus six halo rows per side. Face
 // masks of a row come from shifts of the row and its neighbours, counts from popc.
-// A deterministic block scan over rows gives every row's first face and a compacted
-// list of the rows that have faces; chunks of a batch get their global first face from
-// a decoupled look-back over a device work queue. Faces are written voxel-parallel into
-// a shared-memory staging window in their final byte layout, and the window goes to
-// global memory with TMA bulk copies (cp.async.bulk.global.shared::cta).
+// A deterministic block scan over rows gives every row's first face, the rows that have
+// faces and the voxels that have faces. Chunks of a batch get their global first face
+// either from a decoupled look-back over a device work queue (k_mesh_batch) or from one
+// scan behind a grid barrier (k_mesh_batch_phased). Each warp compacts the faces of a
+// run of voxels, stages them 32 at a time in shared memory in their final byte layout,
+// and sends each batch to global memory with a TMA bulk copy
+// (cp.async.bulk.global.shared::cta), or stores them directly.
 //
 // Reference semantics restated here (Blatko1/wgpu-voxel-engine):
 //   fill rule            src/chunk.rs:35-45     (solid -> GRASS, else AIR)
@@ -1266,9 +1268,6 @@ __device__ __forceinline__ void store_face(void* out0, void* out1, unsigned long
   }
 }
 
-// Direct variant of emit_chunk: no staging window and no barrier; after the same
-// face compaction every lane writes one face record straight to global memory, so the
-// 32 lanes of a warp write 32 consecutive faces.
 // The direct counterpart of warp_send_faces: lane l stores faces l, l + 32, ... of the
 // list straight to global memory.
 template <int N, int LAYOUT>
@@ -1289,6 +1288,8 @@ __device__ __forceinline__ void warp_store_faces(const TablesDev* tab, const uin
   __syncwarp();
 }
 
+// Direct variant of emit_chunk: the same runs and compaction, then every lane writes one
+// face record straight to global memory (32 consecutive faces per warp step).
 template <int N, int LAYOUT>
 __device__ void emit_chunk_direct(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c,
                                   unsigned long long g0, unsigned long long cap, void* out0,
@@ -1399,12 +1400,13 @@ k_mesh_batch(const __grid_constant__ MeshArgs a, const __grid_constant__ TablesD
 // ------------------------------------------------------------------------------------
 // Phased schedule of the fused batch kernel (cooperative launch: the whole grid is
 // resident, so CTAs may wait for one another).
-//  A. CTAs take chunks from the work queue, prepare and count them, and spill the
-//     occupancy + halo rows to a per-chunk scratch (L2-resident) and the face total to
-//     counts[i].
-//  B. Grid barrier. CTA 0 scans counts[] into face_offsets[] and raises the scan flag.
-//  C. CTAs take chunks from the second queue, reload and recount them (row offsets),
-//     wait for the scan flag once, and emit at face_offsets[i].
+//  A. CTAs take chunks from the work queue, prepare and count them, and spill the chunk
+//     state (occupancy, halo, row offsets, row and voxel lists) to a per-chunk slot
+//     (L2-resident) and the face total to counts[i].
+//  B. Grid barrier (it also resets the queue). CTA 0 scans counts[] into face_offsets[]
+//     and raises the scan flag.
+//  C. CTAs take emission items (a chunk, or a segment of one) from the queue again,
+//     reload the chunk state, wait for the scan flag once, and emit at face_offsets[i].
 // There is no chunk-to-chunk dependency inside a phase. The output bytes are the same
 // as the look-back schedule's.
 // ------------------------------------------------------------------------------------
