@@ -591,3 +591,41 @@ def test_raster_matches_oracle(vox, oracle, view):
     got = to_np(rgba, W * H * 4).reshape(H, W, 4)
     assert np.array_equal(got, want)
     ctx.close()
+
+
+@pytest.mark.parametrize("case", range(24))
+def test_randomized_batches_match_oracle(vox, oracle, case):
+    """Seeded random configurations: chunk size, generator, layout, culling, coordinates,
+    neighbour masks, schedule and launch shape all drawn per case."""
+    rng = np.random.default_rng(1000 + case)
+    n = int(rng.choice([8, 16, 32, 64]))
+    kind = str(rng.choice(["height", "height1", "density", "refdensity", "bernoulli"]))
+    layout = int(rng.integers(0, 2))
+    cull = int(rng.integers(0, 2))
+    cfg = gen_cfg(vox, kind, n, layout=layout, cull=cull)
+    m = int(rng.integers(1, 9 if n == 64 else 25))
+    coords = [tuple(int(v) for v in rng.integers(-6, 6, 3)) for _ in range(m)]
+    masks = [int(v) for v in rng.integers(0, 64 if cull else 16, m)]
+    base = int(rng.integers(0, 10_000))
+    w0, w1, woffs = oracle.gen_mesh_batch(cfg, coords, masks, base)
+    total = int(woffs[-1])
+    ctx = ctx_for(vox, cfg)
+    threads = threads_options(n)[int(rng.integers(0, 2))]
+    stage = int(rng.choice([0, 32, 64]))
+    sched = int(rng.integers(0, 2))
+    try:
+        ctx.set_tuning(threads, stage, 0, sched)
+    except vox.VoxError:
+        ctx.set_tuning(threads, 0, 0, sched)  # the staging window does not fit
+    b0, b1 = ctx.sizes.bytes_per_face_out0, ctx.sizes.bytes_per_face_out1
+    o0, o1 = dev_bytes(max(total, 1) * b0), dev_bytes(max(total, 1) * b1)
+    offs = to_dev(np.zeros(m + 1, np.uint64))
+    ctx.gen_mesh_batch(to_dev(np.asarray(coords, np.int32)), to_dev(np.asarray(masks, np.uint8)), m,
+                       o0, o1 if b1 else None, total, offs, chunk_index_base=base)
+    ctx.sync()
+    tag = (n, kind, layout, cull, m, threads, stage, sched)
+    assert np.array_equal(to_np(offs), woffs), tag
+    assert np.array_equal(to_np(o0, total * b0), w0), tag
+    if b1:
+        assert np.array_equal(to_np(o1, total * b1), w1), tag
+    ctx.close()
