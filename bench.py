@@ -152,16 +152,25 @@ def load_peak():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel: str, workload: str):
-    """DRAM bytes per launch recorded from an ncu capture in profiles/ (or None)."""
+def profiled_value(kernel: str, workload: str, key: str = "traffic_bytes_per_launch"):
+    """A per-launch figure recorded from an ncu capture in profiles/ (or None)."""
     path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
     try:
         for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1].strip())
     except OSError:
         pass
     return None
+
+
+def profiled_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch recorded from an ncu capture in profiles/ (or None)."""
+    return profiled_value(kernel, workload)
+
+
+# Warp-instruction issue capacity: 152 SMs x 4 schedulers x 2.07 GHz (nominal).
+ISSUE_PEAK = 152 * 4 * 2.07e9
 
 
 # FP32 operations of one noise sample-octave in the noise formula (the oracle's
@@ -440,6 +449,15 @@ def run_ours(args):
         # p50/p99 request-to-mesh latency of the streaming engine at the serving request
         # rate (real-time 60 frames/s camera), next to the batch throughput above
         line["latency"] = serving_run(args.latency_frames, paced=True)
+    instr = profiled_value(kname, args.workload, "warp_instructions_per_launch")
+    if instr and len(slabs) == 1:
+        # the same launch against the warp-instruction issue rate: for a launch whose
+        # output stays in L2 this, not HBM, is the budget it spends
+        line["issue_roofline"] = {
+            "warp_instructions_per_launch": instr, "achieved": instr / (kernel_ms / 1e3),
+            "peak": ISSUE_PEAK, "unit": "warp instructions/s", "frac": instr / (kernel_ms / 1e3) / ISSUE_PEAK,
+            "peak_source": "nominal (152 SMs x 4 schedulers x 2.07 GHz); instructions from the ncu "
+                           "capture in profiles/"}
     noise = noise_report(wl, cfg, n_all, ms_per_step)
     if noise:
         line["noise_fp32"] = noise
