@@ -63,7 +63,7 @@ def parse_args():
                    help="launch through vox_gen_mesh_batch instead of replaying captured graphs")
     p.add_argument("--tuning", default=None,
                    help="force a launch shape 'threads,stage_faces,ctas_per_sm[,schedule]' "
-                        "(schedule 0 look-back, 1 phased; no autotune)")
+                        "(schedule 0 look-back, 1 phased, 2 overlap; no autotune)")
     p.add_argument("--frames", type=int, default=10000, help="serving workload: frames")
     p.add_argument("--paced", action="store_true", help="serving workload: real-time 60 fps")
     p.add_argument("--latency-frames", type=int, default=300,
@@ -414,7 +414,8 @@ def run_ours(args):
     alg_bytes = total_faces * (b0 + b1) + n_all * (12 + 1) + (n_all + len(slabs)) * 8
     kernel_ms = statistics.median(step_ms)
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
-    kname = "k_mesh_batch_phased" if tuning.get("schedule") == "phased" else "k_mesh_batch"
+    kname = {"phased": "k_mesh_batch_phased", "overlap": "k_mesh_batch_overlap"}.get(
+        tuning.get("schedule"), "k_mesh_batch")
     traffic = profiled_traffic(kname, args.workload)
     line = {
         "metric": METRIC, "value": value, "unit": "chunks/s", "n_gpus": world,

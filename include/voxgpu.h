@@ -235,16 +235,19 @@ typedef struct vox_tuning {
                           buffer and sends them with a TMA bulk copy; 64: the same with
                           two buffers per warp (one fills while the other is sent) */
   int32_t ctas_per_sm; /* resident CTAs per SM of the persistent grid; 0 = as many as fit */
-  int32_t schedule;    /* VOX_SCHEDULE_LOOKBACK or VOX_SCHEDULE_PHASED */
+  int32_t schedule;    /* VOX_SCHEDULE_LOOKBACK, VOX_SCHEDULE_PHASED or VOX_SCHEDULE_OVERLAP */
 } vox_tuning;
 
-/* Schedules of the fused batch kernel (both write the same bytes):
+/* Schedules of the fused batch kernel (all write the same bytes):
  * LOOKBACK: one pass; each chunk's output offset comes from a decoupled look-back over
  *   its predecessors' face counts.
  * PHASED: a cooperative launch in three phases: generate and count every chunk (the
  *   occupancy is kept in a context-owned scratch), scan the counts once, then emit every
- *   chunk at its known offset. No chunk waits for another inside a phase. */
-enum { VOX_SCHEDULE_LOOKBACK = 0, VOX_SCHEDULE_PHASED = 1 };
+ *   chunk at its known offset. No chunk waits for another inside a phase.
+ * OVERLAP: the phases of PHASED without the grid barrier: each chunk's total is published
+ *   as soon as it is counted, and emission takes a chunk's offset from a decoupled
+ *   look-back over the published totals, so emission overlaps the end of generation. */
+enum { VOX_SCHEDULE_LOOKBACK = 0, VOX_SCHEDULE_PHASED = 1, VOX_SCHEDULE_OVERLAP = 2 };
 
 int vox_ctx_get_tuning(vox_ctx* ctx, vox_tuning* out);
 int vox_ctx_set_tuning(vox_ctx* ctx, const vox_tuning* tuning);

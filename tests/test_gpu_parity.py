@@ -14,7 +14,7 @@ from gpu_util import (Pinned, ctx_for, dev_bytes, gpu_gen_mesh, gpu_generate, to
 pytestmark = pytest.mark.gpu
 
 LAYOUTS = [0, 1]  # vertex, instanced
-SCHEDULES = [0, 1]  # look-back, phased (cooperative launch)
+SCHEDULES = [0, 1, 2]  # look-back, phased (cooperative launch), overlap
 
 
 def small_coords():
@@ -474,7 +474,7 @@ def test_every_launch_shape_is_bit_exact(vox, oracle, wlname, sub, layout):
     o0, o1 = dev_bytes(total * b0), dev_bytes(max(total * b1, 16))
     offs = to_dev(np.zeros(len(coords) + 1, np.uint64))
     tried = 0
-    for sched in (vox.SCHEDULE_LOOKBACK, vox.SCHEDULE_PHASED):
+    for sched in (vox.SCHEDULE_LOOKBACK, vox.SCHEDULE_PHASED, vox.SCHEDULE_OVERLAP):
         for threads in threads_options(n):
             for stage in (0, 32, 64):
                 for cps in (0, 2):
@@ -514,7 +514,7 @@ def test_autotune_picks_a_valid_shape(vox, oracle):
     assert t.threads in threads_options(16)
     assert t.stage_faces in (0, 32, 64)
     got = ctx.tuning()
-    assert t.schedule in (vox.SCHEDULE_LOOKBACK, vox.SCHEDULE_PHASED)
+    assert t.schedule in (vox.SCHEDULE_LOOKBACK, vox.SCHEDULE_PHASED, vox.SCHEDULE_OVERLAP)
     assert (got.threads, got.stage_faces, got.ctas_per_sm, got.schedule) == (
         t.threads, t.stage_faces, t.ctas_per_sm, t.schedule)
     o0.fill_(0)
@@ -612,7 +612,7 @@ def test_randomized_batches_match_oracle(vox, oracle, case):
     ctx = ctx_for(vox, cfg)
     threads = threads_options(n)[int(rng.integers(0, 2))]
     stage = int(rng.choice([0, 32, 64]))
-    sched = int(rng.integers(0, 2))
+    sched = int(rng.integers(0, 3))
     try:
         ctx.set_tuning(threads, stage, 0, sched)
     except vox.VoxError:

@@ -44,6 +44,7 @@ struct vox_ctx {
   int spin_limit = kSpinLimit;
   int batch_grid[4] = {0, 0, 0, 0};   // persistent grid per gen mode (look-back kernel)
   int phased_grid[4] = {0, 0, 0, 0};  // co-resident grid per gen mode (phased kernel)
+  int overlap_grid[4] = {0, 0, 0, 0}; // persistent grid per gen mode (overlap kernel)
   int host_grid[4] = {0, 0, 0, 0};    // grid of launches that write host memory (staged)
   // phased schedule: per-chunk occupancy + halo spill and face totals
   uint32_t* d_scratch = nullptr;
@@ -185,28 +186,32 @@ int apply_tuning(vox_ctx* ctx, int topt, int stage_faces, int ctas_per_sm, int s
     return fail(ctx, VOX_ERR_INVALID, "stage_faces must be 0 (direct stores), %d or %d",
                 kStageSingle, kStageDouble);
   if (ctas_per_sm < 0) return fail(ctx, VOX_ERR_INVALID, "ctas_per_sm must be >= 0");
-  if (schedule != VOX_SCHEDULE_LOOKBACK && schedule != VOX_SCHEDULE_PHASED)
-    return fail(ctx, VOX_ERR_INVALID, "schedule must be VOX_SCHEDULE_LOOKBACK or VOX_SCHEDULE_PHASED");
+  if (schedule != VOX_SCHEDULE_LOOKBACK && schedule != VOX_SCHEDULE_PHASED &&
+      schedule != VOX_SCHEDULE_OVERLAP)
+    return fail(ctx, VOX_ERR_INVALID, "unknown schedule");
   const int smem = ks.smem_total(layout, ks.threads[topt], stage_faces);
   if (smem > ctx->max_smem_optin - 256)
     return fail(ctx, VOX_ERR_INVALID, "staging window exceeds shared memory");
-  int grid[4], pgrid[4], hgrid[4];
+  int grid[4], pgrid[4], hgrid[4], ogrid[4];
   const int hsmem = ks.smem_total(layout, ks.threads[topt], kStageSingle);
   for (int gm = 0; gm < 4; ++gm) {
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < 4; ++k) {
       // the phased kernel's grid must be co-resident (cooperative launch): its occupancy
-      // is an upper bound, never exceeded. k = 2: the selected schedule's kernel with one
+      // is an upper bound, never exceeded. k = 3: the selected schedule's kernel with one
       // staging buffer per warp (launches whose outputs are in host memory)
       const void* fn = k == 0 ? ks.batch[gm][layout][topt]
                      : k == 1 ? ks.phased[gm][layout][topt]
-                     : (schedule == VOX_SCHEDULE_PHASED ? ks.phased : ks.batch)[gm][layout][topt];
+                     : k == 2 ? ks.overlap[gm][layout][topt]
+                     : schedule == VOX_SCHEDULE_PHASED  ? ks.phased[gm][layout][topt]
+                     : schedule == VOX_SCHEDULE_OVERLAP ? ks.overlap[gm][layout][topt]
+                                                        : ks.batch[gm][layout][topt];
       int per_sm = 0;
       cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, ks.threads[topt],
-                                                                    k == 2 ? hsmem : smem);
+                                                                    k == 3 ? hsmem : smem);
       if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
       if (per_sm < 1) return fail(ctx, VOX_ERR_INVALID, "kernel does not fit on an SM");
       if (ctas_per_sm > 0) per_sm = std::min(per_sm, ctas_per_sm);
-      (k == 0 ? grid : k == 1 ? pgrid : hgrid)[gm] = per_sm * ctx->num_sms;
+      (k == 0 ? grid : k == 1 ? pgrid : k == 2 ? ogrid : hgrid)[gm] = per_sm * ctx->num_sms;
     }
   }
   ctx->topt = topt;
@@ -216,6 +221,7 @@ int apply_tuning(vox_ctx* ctx, int topt, int stage_faces, int ctas_per_sm, int s
   for (int gm = 0; gm < 4; ++gm) {
     ctx->batch_grid[gm] = grid[gm];
     ctx->phased_grid[gm] = pgrid[gm];
+    ctx->overlap_grid[gm] = ogrid[gm];
     ctx->host_grid[gm] = hgrid[gm];
   }
   return VOX_OK;
@@ -309,18 +315,24 @@ int issue_batch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out, cudaStream_t s
     a.lane_flush = 1;
   }
   void* params[] = {&a, &ctx->h_tables};
-  if (ctx->schedule == VOX_SCHEDULE_PHASED) {
-    const void* fn = ctx->ks->phased[gm][layout][ctx->topt];
-    const int grid = std::max(1, std::min(a.n, host_out ? ctx->host_grid[gm] : ctx->phased_grid[gm]));
+  if (ctx->schedule == VOX_SCHEDULE_PHASED || ctx->schedule == VOX_SCHEDULE_OVERLAP) {
+    const bool phased = ctx->schedule == VOX_SCHEDULE_PHASED;
+    const void* fn = (phased ? ctx->ks->phased : ctx->ks->overlap)[gm][layout][ctx->topt];
+    const int grid = std::max(1, std::min(a.n, host_out ? ctx->host_grid[gm]
+                                             : phased ? ctx->phased_grid[gm] : ctx->overlap_grid[gm]));
     // emission items per chunk: one for small chunks unless there are fewer chunks than
     // CTAs; chunks of 32^3 and up (whose emission dwarfs an item's reload) split until
     // there are about eight items per CTA, which evens out the last wave
     a.split = ctx->cfg.chunk_size >= 32 ? std::max(1, std::min(8, (8 * grid + a.n - 1) / a.n))
                                         : std::max(1, std::min(8, grid / a.n));
     a.split = std::max(1, std::min(a.split, 0x7FFFFFFF / a.n));  // items = n * split fit an int
-    VOX_CUDA(ctx, cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), params, (size_t)smem,
-                                              stream),
-             "cudaLaunchCooperativeKernel");
+    if (phased)
+      VOX_CUDA(ctx, cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), params, (size_t)smem,
+                                                stream),
+               "cudaLaunchCooperativeKernel");
+    else
+      VOX_CUDA(ctx, cudaLaunchKernel(fn, dim3(grid), dim3(threads), params, (size_t)smem, stream),
+               "cudaLaunchKernel");
     return VOX_OK;
   }
   const void* fn = ctx->ks->batch[gm][layout][ctx->topt];
@@ -334,12 +346,14 @@ int issue_batch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out, cudaStream_t s
 // shared-memory buffer and writes them out with plain full-line stores.
 int batch_launch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out = false) {
   int st;
-  if (ctx->schedule == VOX_SCHEDULE_PHASED) {
+  if (ctx->schedule != VOX_SCHEDULE_LOOKBACK) {  // the spill slots of phases A and C
     if ((st = ensure_scratch(ctx, (size_t)a.n)) != VOX_OK) return st;
     a.scratch = ctx->d_scratch;
     a.counts = ctx->d_counts;
+  }
+  if (ctx->schedule == VOX_SCHEDULE_PHASED) {
     ++ctx->launches;
-  } else {
+  } else {  // look-back state words
     if ((st = ensure_state(ctx, (size_t)a.n)) != VOX_OK) return st;
     if ((st = before_batch_launch(ctx)) != VOX_OK) return st;
     a.state = ctx->d_state;
@@ -441,7 +455,8 @@ int vox_ctx_create(const vox_config* cfg, void* stream, vox_ctx** out) {
   for (int gm = 0; gm < 4; ++gm)
     for (int t = 0; t < 2; ++t)
       if ((st = prepare_kernel(ctx, ctx->ks->batch[gm][layout][t], ctx->max_smem_optin)) != VOX_OK ||
-          (st = prepare_kernel(ctx, ctx->ks->phased[gm][layout][t], ctx->max_smem_optin)) != VOX_OK)
+          (st = prepare_kernel(ctx, ctx->ks->phased[gm][layout][t], ctx->max_smem_optin)) != VOX_OK ||
+          (st = prepare_kernel(ctx, ctx->ks->overlap[gm][layout][t], ctx->max_smem_optin)) != VOX_OK)
         return cleanup(st);
   for (int t = 0; t < 2; ++t)
     if ((st = prepare_kernel(ctx, ctx->ks->single[layout][t], ctx->max_smem_optin)) != VOX_OK)
@@ -493,6 +508,7 @@ static int sync_locked(vox_ctx* ctx) {
   ctx->h_ctl->err = 0;
   if (err & ERR_TIMEOUT) {
     ctx->h_ctl->next = 0;
+    ctx->h_ctl->next2 = 0;
     ctx->h_ctl->bar_count = 0;
   }
   VOX_CUDA(ctx, cudaMemcpyAsync(ctx->d_ctl, ctx->h_ctl, sizeof(BatchCtl), cudaMemcpyHostToDevice,
@@ -893,13 +909,15 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
     return true;
   };
   bool go = true;
-  for (int p = 0; p < 2 && go; ++p)
+  for (int p = 0; p < 3 && go; ++p)
     for (int t = 0; t < 2 && go; ++t)
       for (int s : stages) {
         int full_grid = 0;
         for (int c : ctas) {
           if (apply_tuning(ctx, t, s, c, p) != VOX_OK) continue;
-          const int g = p == VOX_SCHEDULE_PHASED ? ctx->phased_grid[ctx->gm] : ctx->batch_grid[ctx->gm];
+          const int g = p == VOX_SCHEDULE_PHASED    ? ctx->phased_grid[ctx->gm]
+                        : p == VOX_SCHEDULE_OVERLAP ? ctx->overlap_grid[ctx->gm]
+                                                    : ctx->batch_grid[ctx->gm];
           if (c == 0) full_grid = g;
           else if (g >= full_grid) continue;  // same grid as c = 0
           if (!(go = time_candidate(p, t, s, c))) break;
@@ -971,13 +989,14 @@ int vox_graph_capture(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8
   a.out1 = d_out1;
   a.cap = cap_faces;
   a.face_offsets = reinterpret_cast<unsigned long long*>(d_face_offsets);
-  if (g->schedule == VOX_SCHEDULE_PHASED) {
+  if (g->schedule != VOX_SCHEDULE_LOOKBACK) {
     if ((e = cudaMalloc(&g->d_scratch, (size_t)n * (size_t)ctx->ks->spill_bytes)) != cudaSuccess ||
         (e = cudaMalloc(&g->d_counts, (size_t)n * sizeof(uint32_t))) != cudaSuccess)
       return bail(cuda_fail(ctx, e, "cudaMalloc(graph scratch)"));
     a.scratch = g->d_scratch;
     a.counts = g->d_counts;
-  } else {
+  }
+  if (g->schedule != VOX_SCHEDULE_PHASED) {
     g->state_bytes = (size_t)n * sizeof(unsigned long long);
     if ((e = cudaMalloc(&g->d_state, g->state_bytes)) != cudaSuccess ||
         (e = cudaMemsetAsync(g->d_state, 0, g->state_bytes, ctx->stream)) != cudaSuccess)

@@ -849,16 +849,17 @@ __device__ uint32_t count_and_scan(ChunkSmem<N, LAYOUT>& s) {
 // back to the nearest inclusive prefix and sums the aggregates in between. Every wait is
 // bounded (spin_limit polls); on timeout the error bit is set and 0 is used.
 constexpr int kLookbackWindow = 128;
+// publish_agg = false: chunk i's aggregate is already published (overlap schedule).
 static __device__ unsigned long long lookback(unsigned long long* state, BatchCtl* ctl,
                                               unsigned epoch, int i, unsigned long long total,
-                                              int spin_limit) {
+                                              int spin_limit, bool publish_agg = true) {
   const int lane = threadIdx.x & 31;
   unsigned long long excl = 0;
   if (i == 0) {
     if (lane == 0) st_relaxed_u64(&state[0], pack_state(epoch, kFlagIncl, total));
     return 0;
   }
-  if (lane == 0) st_relaxed_u64(&state[i], pack_state(epoch, kFlagAgg, total));
+  if (lane == 0 && publish_agg) st_relaxed_u64(&state[i], pack_state(epoch, kFlagAgg, total));
   const unsigned tag = epoch & 0xFFFFFFu;
   const unsigned long long vmask = (1ull << 38) - 1;
   int j = i - 1;
@@ -1622,6 +1623,156 @@ k_mesh_batch_phased(const __grid_constant__ MeshArgs a, const __grid_constant__ 
     if (s_base == ~0ull) break;  // the scan flag never came: give up (error reported)
     if (lo < hi) {
       const vox_chunk_coord c = a.coords[i];
+      if (a.stage_faces > 0)
+        emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch,
+                              a.lane_flush != 0, lo, hi);
+      else emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, lo, hi);
+    }
+    if (t == 0) s_item = next_item;
+    __syncthreads();
+    k = s_item;
+  }
+  if ((t & 31) == 0) bulk_wait_all();  // every lane 0 issued bulk copies
+}
+
+// ------------------------------------------------------------------------------------
+// Overlap schedule of the fused batch kernel: the phases of k_mesh_batch_phased without
+// the grid barrier. Phase A publishes each chunk's face total as a look-back state word
+// (epoch-tagged aggregate) right after its state is spilled; phase C waits only until its
+// own chunk is published, then takes the chunk's offset from a decoupled look-back over
+// the published totals. A CTA draws emission items only after its last generation
+// ticket, and generation never waits, so every wait ends; CTAs move on to emission while
+// others still generate. Normal launch; output bytes identical to the other schedules.
+// ------------------------------------------------------------------------------------
+template <int N, int GM, int LAYOUT, int T>
+__global__ void __launch_bounds__(T)
+k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__ TablesDev tab) {
+  using P = SmemPlan<N, LAYOUT>;
+  constexpr int kFixed16 = (P::kOcc + P::kHalo + P::kRows) / 16;
+  constexpr int kNzOff = P::kOcc + P::kHalo + P::kRows;
+  constexpr int kVlOff = kNzOff + P::kNz;
+  constexpr int kMiscOff = kVlOff + P::kVList;
+  static_assert(P::kSpill == kMiscOff + P::kMisc, "spill layout");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  ChunkSmem<N, LAYOUT> s;
+  s.carve(smem_raw);
+  load_tables<N, LAYOUT>(s, &tab);  // the tables travel as a kernel parameter
+  __shared__ int s_item;
+  __shared__ unsigned s_epoch;
+  __shared__ unsigned long long s_base;
+  __shared__ int s_ok;
+  unsigned char* const spill = reinterpret_cast<unsigned char*>(a.scratch);
+  uint4* const fixed16 = reinterpret_cast<uint4*>(s.occ);  // s.halo, s.rows follow s.occ
+  const int t = threadIdx.x;
+  if (t == 0) {
+    s_epoch = ld_relaxed_u32(&a.ctl->epoch);
+    __threadfence();
+    s_item = (int)atomicAdd(&a.ctl->next, 1u);
+  }
+  __syncthreads();
+  const unsigned epoch = s_epoch;
+
+  // A. prepare + count + spill + publish the chunk's total
+  int i = s_item;
+  for (; i < a.n;) {
+    int next_item = 0;
+    if (t == 0) next_item = (int)atomicAdd(&a.ctl->next, 1u);
+    prepare_chunk<N, GM, LAYOUT, T>(s, a, i, a.coords[i]);
+    const uint32_t total = count_and_scan<N, LAYOUT, T>(s);
+    unsigned char* dst = spill + (unsigned long long)i * P::kSpill;
+    for (int q = t; q < kFixed16; q += T) __stcg(reinterpret_cast<uint4*>(dst) + q, fixed16[q]);
+    const int nzw = (s.misc[0] + 1) >> 1;
+    const int vlw = s.misc[1] > 0 ? (s.misc[1] + 1) >> 1 : 0;
+    for (int q = t; q < nzw; q += T)
+      __stcg(reinterpret_cast<uint32_t*>(dst + kNzOff) + q, reinterpret_cast<const uint32_t*>(s.nz)[q]);
+    for (int q = t; q < vlw; q += T)
+      __stcg(reinterpret_cast<uint32_t*>(dst + kVlOff) + q,
+             reinterpret_cast<const uint32_t*>(s.vlist)[q]);
+    __syncthreads();  // every store of the slot precedes the publication below
+    if (t == 0) {
+      __stcg(reinterpret_cast<int2*>(dst + kMiscOff), make_int2(s.misc[0], s.misc[1]));
+      __threadfence();
+      st_relaxed_u64(&a.state[i], pack_state(epoch, i == 0 ? kFlagIncl : kFlagAgg, total));
+      s_item = next_item;
+    }
+    __syncthreads();
+    i = s_item;
+  }
+  // the last generation ticket of the launch resets its queue
+  if (t == 0 && i == a.n + (int)gridDim.x - 1) a.ctl->next = 0u;
+
+  // C. emission items (chunk k / split, segment k % split) from the second queue
+  const int split = a.split > 0 ? a.split : 1;
+  const int items = a.n * split;
+  if (t == 0) s_item = (int)atomicAdd(&a.ctl->next2, 1u);
+  __syncthreads();
+  int k = s_item;
+  const unsigned tag = epoch & 0xFFFFFFu;
+  while (true) {
+    if (k >= items) {
+      // The last emission ticket of this launch resets the queue and advances the epoch.
+      if (t == 0 && k == items + (int)gridDim.x - 1) {
+        a.ctl->next2 = 0u;
+        a.ctl->epoch = epoch + 1u;
+      }
+      break;
+    }
+    int next_item = 0;
+    if (t == 0) next_item = (int)atomicAdd(&a.ctl->next2, 1u);
+    const int c_i = k / split, seg = k - c_i * split;
+    if (t == 0) {  // wait until the chunk's generation has published its state
+      int spins = 0, ok = 0;
+      while (true) {
+        const unsigned long long w = ld_relaxed_u64(&a.state[c_i]);
+        if (((unsigned)(w >> 40) & 0xFFFFFFu) == tag && ((w >> 38) & 3ull) != 0ull) {
+          ok = 1;
+          break;
+        }
+        if (++spins > a.spin_limit) break;
+        __nanosleep(spins < 8 ? 32 : 256);
+      }
+      if (!ok) atomicOr(&a.ctl->err, ERR_TIMEOUT);
+      __threadfence();
+      s_ok = ok;
+    }
+    __syncthreads();
+    if (!s_ok) break;  // never published (error reported)
+    const unsigned char* src = spill + (unsigned long long)c_i * P::kSpill;
+    for (int q = t; q < kFixed16; q += T) fixed16[q] = __ldcg(reinterpret_cast<const uint4*>(src) + q);
+    if (t == 0) {
+      const int2 m = __ldcg(reinterpret_cast<const int2*>(src + kMiscOff));
+      s.misc[0] = m.x;
+      s.misc[1] = m.y;
+    }
+    __syncthreads();
+    const bool use_list = s.misc[1] >= 0;
+    const int elems = emit_elems(s);
+    const int per = ((elems + split - 1) / split + 31) & ~31;
+    const int lo = min(elems, seg * per), hi = min(elems, lo + per);
+    if (lo < hi) {
+      const int e0 = use_list ? lo : lo / N, e1 = use_list ? hi : (hi - 1) / N + 1;
+      const uint32_t* lsrc = reinterpret_cast<const uint32_t*>(src + (use_list ? kVlOff : kNzOff));
+      uint32_t* ldst = reinterpret_cast<uint32_t*>(use_list ? s.vlist : s.nz);
+      for (int q = (e0 >> 1) + t; q < (e1 + 1) >> 1; q += T) ldst[q] = __ldcg(lsrc + q);
+    }
+    if (t < 32) {
+      const unsigned long long total = s.rows[Shape<N>::R];
+      const unsigned long long excl =
+          lookback(a.state, a.ctl, epoch, c_i, total, a.spin_limit, false);
+      if (t == 0) {
+        s_base = excl;
+        if (seg == 0) {
+          a.face_offsets[c_i] = excl;
+          if (c_i == a.n - 1) {
+            a.face_offsets[a.n] = excl + total;
+            if (excl + total > a.cap) atomicOr(&a.ctl->err, ERR_CAPACITY);
+          }
+        }
+      }
+    }
+    __syncthreads();
+    if (lo < hi) {
+      const vox_chunk_coord c = a.coords[c_i];
       if (a.stage_faces > 0)
         emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch,
                               a.lane_flush != 0, lo, hi);

@@ -19,6 +19,8 @@ static void fill_batch(KernelSet& k) {
   k.batch[GM][L][1] = (const void*)k_mesh_batch<N, GM, L, Shape<N>::T1>;
   k.phased[GM][L][0] = (const void*)k_mesh_batch_phased<N, GM, L, Shape<N>::T0>;
   k.phased[GM][L][1] = (const void*)k_mesh_batch_phased<N, GM, L, Shape<N>::T1>;
+  k.overlap[GM][L][0] = (const void*)k_mesh_batch_overlap<N, GM, L, Shape<N>::T0>;
+  k.overlap[GM][L][1] = (const void*)k_mesh_batch_overlap<N, GM, L, Shape<N>::T1>;
 }
 
 template <int N>

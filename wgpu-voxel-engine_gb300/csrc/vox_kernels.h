@@ -12,6 +12,7 @@ struct KernelSet {
   int threads[2];               // the two CTA sizes the meshing kernels exist in
   const void* batch[4][2][2];   // k_mesh_batch<N, gen mode, layout, threads[t]>
   const void* phased[4][2][2];  // k_mesh_batch_phased<N, gen mode, layout, threads[t]>
+  const void* overlap[4][2][2]; // k_mesh_batch_overlap<N, gen mode, layout, threads[t]>
   const void* single[2][2];     // k_mesh_single<N, layout, threads[t]>
   const void* generate[4];      // k_generate<N, gen mode, gen_threads> (index 0 unused)
   int gen_threads;

@@ -44,7 +44,8 @@ struct BatchCtl {
   unsigned int bar_count;  // grid barrier: CTAs arrived (reset by the last arriver)
   unsigned int bar_gen;    // grid barrier: generation, advanced by the last arriver
   unsigned int scan_flag;  // phased kernel: the generation whose offset scan is complete
-  unsigned int pad[2];
+  unsigned int next2;      // overlap kernel: work-queue ticket of the emission items
+  unsigned int pad;
 };
 
 struct MeshArgs {

@@ -30,7 +30,7 @@ VOX_ERR_TIMEOUT, VOX_ERR_CAPACITY, VOX_ERR_NO_DEVICE = 4, 5, 6
 GEN_HEIGHTMAP, GEN_DENSITY, GEN_BERNOULLI = 0, 1, 2
 CULL_REFERENCE, CULL_FULL6 = 0, 1
 LAYOUT_VERTEX, LAYOUT_INSTANCED = 0, 1
-SCHEDULE_LOOKBACK, SCHEDULE_PHASED = 0, 1
+SCHEDULE_LOOKBACK, SCHEDULE_PHASED, SCHEDULE_OVERLAP = 0, 1, 2
 VOX_REQ_UNKNOWN, VOX_REQ_PENDING, VOX_REQ_RESIDENT = 0, 1, 2
 # TEXTURE_INDEX_LIST row of GRASS (src/texture.rs:240-243), by face slot L R Bk F Up Down.
 GRASS_TEXTURES = (0, 0, 0, 0, 2, 1)
@@ -71,7 +71,8 @@ class Tuning(ctypes.Structure):
     def as_dict(self):
         return {"threads": self.threads, "stage_faces": self.stage_faces,
                 "ctas_per_sm": self.ctas_per_sm,
-                "schedule": "phased" if self.schedule == SCHEDULE_PHASED else "lookback"}
+                "schedule": {SCHEDULE_PHASED: "phased", SCHEDULE_OVERLAP: "overlap"}.get(
+                    self.schedule, "lookback")}
 
 
 class ServeConfig(ctypes.Structure):
