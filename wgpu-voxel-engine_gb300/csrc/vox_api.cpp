@@ -160,9 +160,9 @@ int gen_mode_of(int kind) {
 }
 
 // The default tuning (before any autotuning), the shape that measured fastest on the
-// heightmap, density and stress batches: the phased schedule with one staging buffer per
+// heightmap, density and stress batches: the overlap schedule with one staging buffer per
 // warp, and the larger CTA size for chunks up to 32^3.
-constexpr int kDefaultSchedule = VOX_SCHEDULE_PHASED;
+constexpr int kDefaultSchedule = VOX_SCHEDULE_OVERLAP;
 int default_topt(int chunk_size) { return chunk_size <= 32 ? 1 : 0; }
 
 // Allows `fn` up to `smem` bytes of dynamic shared memory (capped at what the device
