@@ -183,17 +183,22 @@ NOISE_OPS = {2: 2 + 2 + 14 + 2 + 4 * 3 + 3 * 3 + 2 + 4, 3: 3 + 3 + 21 + 3 + 8 * 
 FP32_OPS_NOMINAL = 152 * 128 * 2.07e9
 
 
-def noise_report(wl, cfg, n_chunks, ms_per_step):
+def noise_report(wl, cfg, masks, ms_per_step):
     """Algorithmic FP32 throughput of the noise in one step: samples x octaves x ops."""
     N = cfg.chunk_size
     g = cfg.gen
+    n_chunks = len(masks)
     if g.kind == 0:    # heightmap: 2-D noise per column, (N + 2)^2 - 4 columns with halo
         samples, dim = (N + 2) ** 2 - 4, 2
-    elif g.kind == 1:  # density: 3-D noise per voxel and halo voxel
-        samples, dim = N ** 3 + 6 * N * N, 3
+        total = n_chunks * samples
+    elif g.kind == 1:  # density: 3-D noise per voxel and per halo voxel of a loaded neighbour
+        samples, dim = N ** 3, 3
+        used = 0x3F if cfg.cull_mode == 1 else 0x0F
+        total = n_chunks * samples + sum(bin(m & used).count("1") for m in masks) * N * N
+        samples = total / n_chunks
     else:
         return None
-    ops = n_chunks * samples * g.octaves * NOISE_OPS[dim]
+    ops = total * g.octaves * NOISE_OPS[dim]
     achieved = ops / (ms_per_step / 1e3)
     return {"samples_per_chunk": samples, "octaves": g.octaves, "ops_per_sample_octave": NOISE_OPS[dim],
             "achieved_tops": achieved / 1e12, "peak_tops": FP32_OPS_NOMINAL / 1e12,
@@ -332,6 +337,8 @@ def run_ours(args):
             tuning = ctx.autotune(d_coords[a:b], d_mask[a:b], b - a, o0, o1, cap, d_offs[a:b + 1],
                                   chunk_index_base=wl.index_base + a, iters=args.tune_iters)
     tuning = ctx.tuning().as_dict() | {"autotuned": tuning is not None}
+    if rank == 0:
+        print(f"launch shape: {tuning}", file=sys.stderr, flush=True)
 
     # each slab's launch captured once as a CUDA graph and replayed every step
     graphs = []
@@ -398,6 +405,10 @@ def run_ours(args):
     if rank == 0 and len(slabs) == 1 and not wl.isolated:
         rebuild = mesh_from_occupancy(ctx, wl, cfg, d_coords, n_all, o0, o1, cap, total_faces,
                                       stream, flush, args, torch, np)
+    # the generation kernel alone (heightmap and density generators)
+    gen_alone = None
+    if rank == 0 and len(slabs) == 1:
+        gen_alone = noise_kernel(ctx, wl, cfg, d_coords, n_all, stream, flush, args, torch)
     # end to end through the host-pointer entry point (pinned buffers); the stress output
     # (49 GB per 1024 chunks) is sampled on its first 64 chunks
     e2e = None
@@ -446,6 +457,8 @@ def run_ours(args):
         line["e2e"] = e2e
     if rebuild:
         line["mesh_from_occupancy"] = rebuild
+    if gen_alone:
+        line["noise_kernel"] = gen_alone
     if rank == 0 and world == 1 and args.latency_frames > 0 and args.workload == "heightmap":
         # p50/p99 request-to-mesh latency of the streaming engine at the serving request
         # rate (real-time 60 frames/s camera), next to the batch throughput above
@@ -459,7 +472,7 @@ def run_ours(args):
             "peak": ISSUE_PEAK, "unit": "warp instructions/s", "frac": instr / (kernel_ms / 1e3) / ISSUE_PEAK,
             "peak_source": "nominal (152 SMs x 4 schedulers x 2.07 GHz); instructions from the ncu "
                            "capture in profiles/"}
-    noise = noise_report(wl, cfg, n_all, ms_per_step)
+    noise = noise_report(wl, cfg, masks, ms_per_step)
     if noise:
         line["noise_fp32"] = noise
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -520,6 +533,43 @@ def plain_per_chunk(ctx, wl, cfg, d_coords, stream, args, b0, b1, torch, np):
     ms = t0.elapsed_time(t1) / args.plain_steps
     return {"value": k / (ms / 1e3), "unit": "chunks/s", "chunks_per_pass": k,
             "launches_per_chunk": 2, "ms_per_pass": ms}
+
+
+def noise_kernel(ctx, wl, cfg, d_coords, n, stream, flush, args, torch):
+    """The generation kernel alone (Chunk::new, src/chunk.rs:21-46): vox_generate writes the
+    occupancy of every chunk (no halo) to a device pool; its noise FP32 work is samples x
+    octaves x the formula's operation count, against the nominal FP32 instruction rate."""
+    g = cfg.gen
+    if g.kind not in (0, 1):
+        return None
+    N = cfg.chunk_size
+    samples, dim = (N * N, 2) if g.kind == 0 else (N ** 3, 3)
+    pool = torch.empty(n * ctx.sizes.occ_words_per_chunk, dtype=torch.int32, device="cuda")
+    steps = max(3, args.steps // 4)
+    torch.cuda.synchronize()
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            ctx.generate(d_coords, n, pool, chunk_index_base=wl.index_base)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(steps)]
+        for k in range(steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            ctx.generate(d_coords, n, pool, chunk_index_base=wl.index_base)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    assert ctx.sync(raise_on_error=False) == 0
+    ms = statistics.median(a.elapsed_time(b) for a, b in ev)
+    ops = n * samples * g.octaves * NOISE_OPS[dim]
+    achieved = ops / (ms / 1e3)
+    return {"kernel": "k_generate", "ms": ms, "steps": steps, "chunks": n,
+            "samples_per_chunk": samples, "octaves": g.octaves,
+            "ops_per_sample_octave": NOISE_OPS[dim], "achieved_tops": achieved / 1e12,
+            "peak_tops": FP32_OPS_NOMINAL / 1e12,
+            "peak_source": "nominal FP32 instruction rate (FMA contraction off)",
+            "frac": achieved / FP32_OPS_NOMINAL,
+            "occupancy_bytes": n * ctx.sizes.occ_words_per_chunk * 4,
+            "api": "vox_generate (occupancy to a device pool, L2 flushed before each step)"}
 
 
 def mesh_from_occupancy(ctx, wl, cfg, d_coords, n, o0, o1, cap, total_faces, stream, flush, args,

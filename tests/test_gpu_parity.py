@@ -264,25 +264,35 @@ def test_chunk_bytes_independent_of_batch(vox, oracle):
         assert np.array_equal(a1[lo * 24:hi * 24], s1)
 
 
-def test_repeat_launches_identical(vox):
-    """Back-to-back launches on one context (epoch-tagged look-back) give the same bytes."""
+@pytest.mark.parametrize("schedule", SCHEDULES)
+def test_repeat_launches_identical(vox, schedule):
+    """Back-to-back launches on one context (epoch-tagged look-back, queue words reset by
+    the last ticket) give the same bytes: 300 launches without a host sync in between,
+    direct and as graph replays, as in a timed loop."""
     wl = vox.workload("heightmap")
     cfg = wl.config()
     ctx = ctx_for(vox, cfg)
+    use_schedule(ctx, schedule)
     n = len(wl.coords)
     d_coords = to_dev(np.asarray(wl.coords, np.int32))
     d_mask = to_dev(np.asarray(wl.masks(), np.uint8))
     cap = 3_000_000
     o0, o1 = dev_bytes(cap * 96), dev_bytes(cap * 24)
     offs = to_dev(np.zeros(n + 1, np.uint64))
+    g = ctx.capture_graph(d_coords, d_mask, n, o0, o1, cap, offs)
     digests = []
-    for _ in range(5):
-        ctx.gen_mesh_batch(d_coords, d_mask, n, o0, o1, cap, offs)
-        ctx.sync()
+    for rep in range(6):
+        for _ in range(50):
+            if rep % 2:
+                g.launch()
+            else:
+                ctx.gen_mesh_batch(d_coords, d_mask, n, o0, o1, cap, offs)
+        assert ctx.sync(raise_on_error=False) == vox.VOX_OK, rep
         total = int(to_np(offs)[n])
         digests.append((total, hash(to_np(o0, total * 96).tobytes()),
                         hash(to_np(o1, total * 24).tobytes())))
     assert len(set(digests)) == 1
+    g.close()
     ctx.close()
 
 

@@ -1704,6 +1704,7 @@ k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__
   // C. emission items (chunk k / split, segment k % split) from the second queue
   const int split = a.split > 0 ? a.split : 1;
   const int items = a.n * split;
+  __syncthreads();  // every thread has read its last generation ticket from s_item
   if (t == 0) s_item = (int)atomicAdd(&a.ctl->next2, 1u);
   __syncthreads();
   int k = s_item;
