@@ -206,6 +206,11 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
   asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
 __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
   asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
@@ -1660,7 +1665,6 @@ k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__
   __shared__ int s_item;
   __shared__ unsigned s_epoch;
   __shared__ unsigned long long s_base;
-  __shared__ int s_ok;
   unsigned char* const spill = reinterpret_cast<unsigned char*>(a.scratch);
   uint4* const fixed16 = reinterpret_cast<uint4*>(s.occ);  // s.halo, s.rows follow s.occ
   const int t = threadIdx.x;
@@ -1721,57 +1725,69 @@ k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__
     int next_item = 0;
     if (t == 0) next_item = (int)atomicAdd(&a.ctl->next2, 1u);
     const int c_i = k / split, seg = k - c_i * split;
-    if (t == 0) {  // wait until the chunk's generation has published its state
-      int spins = 0, ok = 0;
-      while (true) {
-        const unsigned long long w = ld_relaxed_u64(&a.state[c_i]);
-        if (((unsigned)(w >> 40) & 0xFFFFFFu) == tag && ((w >> 38) & 3ull) != 0ull) {
-          ok = 1;
-          break;
-        }
-        if (++spins > a.spin_limit) break;
-        __nanosleep(spins < 8 ? 32 : 256);
-      }
-      if (!ok) atomicOr(&a.ctl->err, ERR_TIMEOUT);
-      __threadfence();
-      s_ok = ok;
-    }
-    __syncthreads();
-    if (!s_ok) break;  // never published (error reported)
     const unsigned char* src = spill + (unsigned long long)c_i * P::kSpill;
-    for (int q = t; q < kFixed16; q += T) fixed16[q] = __ldcg(reinterpret_cast<const uint4*>(src) + q);
-    if (t == 0) {
-      const int2 m = __ldcg(reinterpret_cast<const int2*>(src + kMiscOff));
-      s.misc[0] = m.x;
-      s.misc[1] = m.y;
+    // Every thread waits for the chunk's published state with an acquire load, so its own
+    // reads of the spill slot below are ordered after the slot's stores (no fence and no
+    // barrier before the reload). The waits are bounded; the barrier below combines them.
+    unsigned long long w = 0;
+    int ok = 0;
+    for (int spins = 0;;) {
+      w = ld_acquire_u64(&a.state[c_i]);
+      if (((unsigned)(w >> 40) & 0xFFFFFFu) == tag && ((w >> 38) & 3ull) != 0ull) {
+        ok = 1;
+        break;
+      }
+      if (++spins > a.spin_limit) break;
+      __nanosleep(spins < 8 ? 32 : 256);
     }
-    __syncthreads();
-    const bool use_list = s.misc[1] >= 0;
-    const int elems = emit_elems(s);
-    const int per = ((elems + split - 1) / split + 31) & ~31;
-    const int lo = min(elems, seg * per), hi = min(elems, lo + per);
-    if (lo < hi) {
-      const int e0 = use_list ? lo : lo / N, e1 = use_list ? hi : (hi - 1) / N + 1;
-      const uint32_t* lsrc = reinterpret_cast<const uint32_t*>(src + (use_list ? kVlOff : kNzOff));
-      uint32_t* ldst = reinterpret_cast<uint32_t*>(use_list ? s.vlist : s.nz);
-      for (int q = (e0 >> 1) + t; q < (e1 + 1) >> 1; q += T) ldst[q] = __ldcg(lsrc + q);
-    }
+    ok = __all_sync(0xffffffffu, ok);  // warp-uniform (warp 0's look-back needs every lane)
+    if (!ok && (t & 31) == 0) atomicOr(&a.ctl->err, ERR_TIMEOUT);
+    // Warp 0 takes the chunk's offset by look-back over the published totals while the
+    // other warps reload the chunk's state (a one-warp CTA does both, in turn).
+    constexpr int TR = T > 32 ? T - 32 : 32;  // reloading threads
+    const int tr = T > 32 ? t - 32 : t;
     if (t < 32) {
-      const unsigned long long total = s.rows[Shape<N>::R];
-      const unsigned long long excl =
-          lookback(a.state, a.ctl, epoch, c_i, total, a.spin_limit, false);
-      if (t == 0) {
-        s_base = excl;
-        if (seg == 0) {
-          a.face_offsets[c_i] = excl;
-          if (c_i == a.n - 1) {
-            a.face_offsets[a.n] = excl + total;
-            if (excl + total > a.cap) atomicOr(&a.ctl->err, ERR_CAPACITY);
+      if (ok) {
+        const unsigned long long total = __ldcg(
+            reinterpret_cast<const uint32_t*>(src + P::kOcc + P::kHalo) + Shape<N>::R);
+        const unsigned long long excl =
+            lookback(a.state, a.ctl, epoch, c_i, total, a.spin_limit, false);
+        if (t == 0) {
+          s_base = excl;
+          if (seg == 0) {
+            a.face_offsets[c_i] = excl;
+            if (c_i == a.n - 1) {
+              a.face_offsets[a.n] = excl + total;
+              if (excl + total > a.cap) atomicOr(&a.ctl->err, ERR_CAPACITY);
+            }
           }
         }
       }
     }
-    __syncthreads();
+    if (ok && tr >= 0) {
+      const int2 m = __ldcg(reinterpret_cast<const int2*>(src + kMiscOff));
+      if (tr == 0) {
+        s.misc[0] = m.x;
+        s.misc[1] = m.y;
+      }
+      if (m.x > 0) {  // rows with faces: an empty chunk needs no state
+        for (int q = tr; q < kFixed16; q += TR) fixed16[q] = __ldcg(reinterpret_cast<const uint4*>(src) + q);
+        const bool use_list = m.y >= 0;
+        const int elems = use_list ? m.y : m.x * N;
+        const int per = ((elems + split - 1) / split + 31) & ~31;
+        const int lo = min(elems, seg * per), hi = min(elems, lo + per);
+        if (lo < hi) {
+          const int e0 = use_list ? lo : lo / N, e1 = use_list ? hi : (hi - 1) / N + 1;
+          const uint32_t* lsrc = reinterpret_cast<const uint32_t*>(src + (use_list ? kVlOff : kNzOff));
+          uint32_t* ldst = reinterpret_cast<uint32_t*>(use_list ? s.vlist : s.nz);
+          for (int q = (e0 >> 1) + tr; q < (e1 + 1) >> 1; q += TR) ldst[q] = __ldcg(lsrc + q);
+        }
+      }
+    }
+    if (!__syncthreads_and(ok)) break;  // never published (error reported)
+    const int elems = emit_elems(s);
+    const int per = ((elems + split - 1) / split + 31) & ~31;
+    const int lo = min(elems, seg * per), hi = min(elems, lo + per);
     if (lo < hi) {
       const vox_chunk_coord c = a.coords[c_i];
       if (a.stage_faces > 0)
