@@ -503,13 +503,15 @@ static int sync_locked(vox_ctx* ctx) {
   VOX_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
   const unsigned err = ctx->h_ctl->err;
   if (err == 0) return VOX_OK;
-  // Clear the error bits. After a timeout a phased launch may have left its queue and its
-  // barrier count mid-way: reset them too (the epoch and generation words stay).
+  // Clear the error bits. After a timeout a launch may have left its queue words and its
+  // barrier count mid-way: reset them too, and move to a fresh look-back epoch, so that no
+  // state word the failed launch published can match a later launch's tag.
   ctx->h_ctl->err = 0;
   if (err & ERR_TIMEOUT) {
     ctx->h_ctl->next = 0;
     ctx->h_ctl->next2 = 0;
     ctx->h_ctl->bar_count = 0;
+    ctx->h_ctl->epoch += 1;
   }
   VOX_CUDA(ctx, cudaMemcpyAsync(ctx->d_ctl, ctx->h_ctl, sizeof(BatchCtl), cudaMemcpyHostToDevice,
                                 ctx->stream),

@@ -1750,8 +1750,13 @@ k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__
       if (ok) {
         const unsigned long long total = __ldcg(
             reinterpret_cast<const uint32_t*>(src + P::kOcc + P::kHalo) + Shape<N>::R);
+        // An inclusive state (chunk 0, or a segment of a chunk whose offset another item
+        // has already found) gives the offset at once.
+        w = __shfl_sync(0xffffffffu, w, 0);
         const unsigned long long excl =
-            lookback(a.state, a.ctl, epoch, c_i, total, a.spin_limit, false);
+            ((w >> 38) & 3ull) == kFlagIncl
+                ? (w & ((1ull << 38) - 1)) - total
+                : lookback(a.state, a.ctl, epoch, c_i, total, a.spin_limit, false);
         if (t == 0) {
           s_base = excl;
           if (seg == 0) {

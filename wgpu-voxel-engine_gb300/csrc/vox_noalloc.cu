@@ -239,14 +239,26 @@ extern "C" int vox_gen_mesh_batch_noalloc(const vox_config* cfg, void* stream,
     std::fprintf(stderr, "voxgpu: launch failed: %s\n", cudaGetErrorString(e));
     return VOX_ERR_CUDA;
   }
-  unsigned err = 0;
-  if (cudaMemcpyAsync(&err, &scratch->ctl.err, sizeof err, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+  BatchCtl ctl;
+  if (cudaMemcpyAsync(&ctl, &scratch->ctl, sizeof ctl, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess) {
     const cudaError_t e = cudaGetLastError();
     std::fprintf(stderr, "voxgpu: %s\n", cudaGetErrorString(e));
     return VOX_ERR_CUDA;
   }
-  if (err & ERR_TIMEOUT) return VOX_ERR_TIMEOUT;
+  const unsigned err = ctl.err;
+  if (err & ERR_TIMEOUT) {
+    // a fresh look-back epoch: no state word of the failed launch can match a later tag
+    ctl.epoch += 1;
+    if (cudaMemcpyAsync(&scratch->ctl.epoch, &ctl.epoch, sizeof ctl.epoch, cudaMemcpyHostToDevice,
+                        st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+      const cudaError_t e = cudaGetLastError();
+      std::fprintf(stderr, "voxgpu: %s\n", cudaGetErrorString(e));
+      return VOX_ERR_CUDA;
+    }
+    return VOX_ERR_TIMEOUT;
+  }
   if (err & ERR_CAPACITY) return VOX_ERR_CAPACITY;
   return VOX_OK;
 }
