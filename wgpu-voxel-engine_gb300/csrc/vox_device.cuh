@@ -1219,10 +1219,14 @@ __device__ __forceinline__ void emit_runs(ChunkSmem<N, LAYOUT>& s, int lo, int h
   if (have > 0) send(list, have, first_have);
 }
 
+// wait_read = false: the caller's next use of the staging area is another emit_chunk. With
+// one buffer per warp its first send waits for every earlier copy's read of that buffer,
+// so the warp need not wait for its last copies here (with two buffers it still does: the
+// next call starts again at buffer 0, which the last copy may still be reading).
 template <int N, int LAYOUT>
 __device__ void emit_chunk(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c, unsigned long long g0,
                            unsigned long long cap, void* out0, void* out1, int nbuf,
-                           bool lane_flush, int lo, int hi) {
+                           bool lane_flush, int lo, int hi, bool wait_read = true) {
   constexpr int kBuf = warp_buf_bytes<LAYOUT>();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned char* bufs = s.stage + (size_t)warp * nbuf * kBuf;
@@ -1231,8 +1235,10 @@ __device__ void emit_chunk(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c, unsigned 
     warp_send_faces<N, LAYOUT>(s.tab, list, nf, first, c, g0, cap, out0, out1, bufs, nbuf,
                                lane_flush, b);
   });
-  if (lane == 0) bulk_wait_read_all();
-  __syncwarp();
+  if (wait_read || nbuf != 1) {
+    if (lane == 0) bulk_wait_read_all();
+    __syncwarp();
+  }
 }
 
 // Writes one face record straight to global memory (face index g).
@@ -1630,7 +1636,7 @@ k_mesh_batch_phased(const __grid_constant__ MeshArgs a, const __grid_constant__ 
       const vox_chunk_coord c = a.coords[i];
       if (a.stage_faces > 0)
         emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch,
-                              a.lane_flush != 0, lo, hi);
+                              a.lane_flush != 0, lo, hi, false);
       else emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, lo, hi);
     }
     if (t == 0) s_item = next_item;
@@ -1642,13 +1648,36 @@ k_mesh_batch_phased(const __grid_constant__ MeshArgs a, const __grid_constant__ 
 
 // ------------------------------------------------------------------------------------
 // Overlap schedule of the fused batch kernel: the phases of k_mesh_batch_phased without
-// the grid barrier. Phase A publishes each chunk's face total as a look-back state word
-// (epoch-tagged aggregate) right after its state is spilled; phase C waits only until its
-// own chunk is published, then takes the chunk's offset from a decoupled look-back over
-// the published totals. A CTA draws emission items only after its last generation
-// ticket, and generation never waits, so every wait ends; CTAs move on to emission while
-// others still generate. Normal launch; output bytes identical to the other schedules.
+// the grid barrier, interleaved on one work queue. A generation item (A) prepares and
+// counts a chunk, spills its state and publishes its face total as an epoch-tagged
+// aggregate look-back state; an emission item (C) waits until its own chunk is published,
+// takes the chunk's offset from a decoupled look-back over the published totals, reloads
+// the chunk state and emits. Ticket order (overlap_ticket): A(0..L-1), then A(L+m) and
+// C(m) alternately while generation items remain, then the remaining emission items.
+// Every wait is for an item with a smaller ticket, which a running CTA holds or has
+// finished, and generation items never wait, so every wait ends without co-residency:
+// a normal launch. L = n (all generation first) suits launches bound by issue; a smaller L
+// starts emission early, which hides generation behind a slow output (host memory).
 // ------------------------------------------------------------------------------------
+
+// Item of ticket t: returns 0 (generation, idx = chunk), 1 (emission, idx = item) or 2
+// (past the end). n chunks, `items` emission items (>= n), lag L in [0, n].
+__device__ __forceinline__ int overlap_ticket(unsigned t, unsigned n, unsigned items, unsigned L,
+                                              unsigned& idx) {
+  if (t < L) {
+    idx = t;
+    return 0;
+  }
+  const unsigned P = n - L;  // interleaved pairs
+  const unsigned u = t - L;
+  if (u < 2u * P) {
+    idx = (u & 1u) ? (u >> 1) : L + (u >> 1);
+    return (u & 1u) ? 1 : 0;
+  }
+  idx = P + (u - 2u * P);
+  return idx < items ? 1 : 2;
+}
+
 template <int N, int GM, int LAYOUT, int T>
 __global__ void __launch_bounds__(T)
 k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__ TablesDev tab) {
@@ -1662,7 +1691,7 @@ k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__
   ChunkSmem<N, LAYOUT> s;
   s.carve(smem_raw);
   load_tables<N, LAYOUT>(s, &tab);  // the tables travel as a kernel parameter
-  __shared__ int s_item;
+  __shared__ unsigned s_item;
   __shared__ unsigned s_epoch;
   __shared__ unsigned long long s_base;
   unsigned char* const spill = reinterpret_cast<unsigned char*>(a.scratch);
@@ -1671,83 +1700,85 @@ k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__
   if (t == 0) {
     s_epoch = ld_relaxed_u32(&a.ctl->epoch);
     __threadfence();
-    s_item = (int)atomicAdd(&a.ctl->next, 1u);
+    s_item = atomicAdd(&a.ctl->next, 1u);
   }
   __syncthreads();
   const unsigned epoch = s_epoch;
-
-  // A. prepare + count + spill + publish the chunk's total
-  int i = s_item;
-  for (; i < a.n;) {
-    int next_item = 0;
-    if (t == 0) next_item = (int)atomicAdd(&a.ctl->next, 1u);
-    prepare_chunk<N, GM, LAYOUT, T>(s, a, i, a.coords[i]);
-    const uint32_t total = count_and_scan<N, LAYOUT, T>(s);
-    unsigned char* dst = spill + (unsigned long long)i * P::kSpill;
-    for (int q = t; q < kFixed16; q += T) __stcg(reinterpret_cast<uint4*>(dst) + q, fixed16[q]);
-    const int nzw = (s.misc[0] + 1) >> 1;
-    const int vlw = s.misc[1] > 0 ? (s.misc[1] + 1) >> 1 : 0;
-    for (int q = t; q < nzw; q += T)
-      __stcg(reinterpret_cast<uint32_t*>(dst + kNzOff) + q, reinterpret_cast<const uint32_t*>(s.nz)[q]);
-    for (int q = t; q < vlw; q += T)
-      __stcg(reinterpret_cast<uint32_t*>(dst + kVlOff) + q,
-             reinterpret_cast<const uint32_t*>(s.vlist)[q]);
-    __syncthreads();  // every store of the slot precedes the publication below
-    if (t == 0) {
-      __stcg(reinterpret_cast<int2*>(dst + kMiscOff), make_int2(s.misc[0], s.misc[1]));
-      __threadfence();
-      st_relaxed_u64(&a.state[i], pack_state(epoch, i == 0 ? kFlagIncl : kFlagAgg, total));
-      s_item = next_item;
-    }
-    __syncthreads();
-    i = s_item;
-  }
-  // the last generation ticket of the launch resets its queue
-  if (t == 0 && i == a.n + (int)gridDim.x - 1) a.ctl->next = 0u;
-
-  // C. emission items (chunk k / split, segment k % split) from the second queue
-  const int split = a.split > 0 ? a.split : 1;
-  const int items = a.n * split;
-  __syncthreads();  // every thread has read its last generation ticket from s_item
-  if (t == 0) s_item = (int)atomicAdd(&a.ctl->next2, 1u);
-  __syncthreads();
-  int k = s_item;
   const unsigned tag = epoch & 0xFFFFFFu;
+  const unsigned n = (unsigned)a.n;
+  const int split = a.split > 0 ? a.split : 1;
+  const unsigned items = n * (unsigned)split;
+  const unsigned lag = a.lag < 0 || (unsigned)a.lag > n ? n : (unsigned)a.lag;
+  const unsigned last_ticket = n + items + gridDim.x - 1u;
+  bool stage_busy = false;  // bulk copies of this CTA may still read the staging area
+  unsigned tk = s_item;
   while (true) {
-    if (k >= items) {
-      // The last emission ticket of this launch resets the queue and advances the epoch.
-      if (t == 0 && k == items + (int)gridDim.x - 1) {
-        a.ctl->next2 = 0u;
+    unsigned idx;
+    const int kind = overlap_ticket(tk, n, items, lag, idx);
+    if (kind == 2) {
+      // The last ticket of this launch resets the queue and advances the epoch.
+      if (t == 0 && tk == last_ticket) {
+        a.ctl->next = 0u;
         a.ctl->epoch = epoch + 1u;
       }
       break;
     }
-    int next_item = 0;
-    if (t == 0) next_item = (int)atomicAdd(&a.ctl->next2, 1u);
-    const int c_i = k / split, seg = k - c_i * split;
-    const unsigned char* src = spill + (unsigned long long)c_i * P::kSpill;
-    // Every thread waits for the chunk's published state with an acquire load, so its own
-    // reads of the spill slot below are ordered after the slot's stores (no fence and no
-    // barrier before the reload). The waits are bounded; the barrier below combines them.
-    unsigned long long w = 0;
-    int ok = 0;
-    for (int spins = 0;;) {
-      w = ld_acquire_u64(&a.state[c_i]);
-      if (((unsigned)(w >> 40) & 0xFFFFFFu) == tag && ((w >> 38) & 3ull) != 0ull) {
-        ok = 1;
-        break;
+    // the next ticket is drawn now and used after this item, so the atomic's latency
+    // overlaps the item's work
+    unsigned next_tk = 0;
+    if (t == 0) next_tk = atomicAdd(&a.ctl->next, 1u);
+    if (kind == 0) {
+      // A. prepare + count + spill + publish the chunk's total. Generation reuses the
+      // staging area as scratch: wait until the earlier copies have read it.
+      if (stage_busy) {
+        if ((t & 31) == 0) bulk_wait_read_all();
+        __syncthreads();
+        stage_busy = false;
       }
-      if (++spins > a.spin_limit) break;
-      __nanosleep(spins < 8 ? 32 : 256);
-    }
-    ok = __all_sync(0xffffffffu, ok);  // warp-uniform (warp 0's look-back needs every lane)
-    if (!ok && (t & 31) == 0) atomicOr(&a.ctl->err, ERR_TIMEOUT);
-    // Warp 0 takes the chunk's offset by look-back over the published totals while the
-    // other warps reload the chunk's state (a one-warp CTA does both, in turn).
-    constexpr int TR = T > 32 ? T - 32 : 32;  // reloading threads
-    const int tr = T > 32 ? t - 32 : t;
-    if (t < 32) {
-      if (ok) {
+      const int i = (int)idx;
+      prepare_chunk<N, GM, LAYOUT, T>(s, a, i, a.coords[i]);
+      const uint32_t total = count_and_scan<N, LAYOUT, T>(s);
+      unsigned char* dst = spill + (unsigned long long)i * P::kSpill;
+      for (int q = t; q < kFixed16; q += T) __stcg(reinterpret_cast<uint4*>(dst) + q, fixed16[q]);
+      const int nzw = (s.misc[0] + 1) >> 1;
+      const int vlw = s.misc[1] > 0 ? (s.misc[1] + 1) >> 1 : 0;
+      for (int q = t; q < nzw; q += T)
+        __stcg(reinterpret_cast<uint32_t*>(dst + kNzOff) + q, reinterpret_cast<const uint32_t*>(s.nz)[q]);
+      for (int q = t; q < vlw; q += T)
+        __stcg(reinterpret_cast<uint32_t*>(dst + kVlOff) + q,
+               reinterpret_cast<const uint32_t*>(s.vlist)[q]);
+      __syncthreads();  // every store of the slot precedes the publication below
+      if (t == 0) {
+        __stcg(reinterpret_cast<int2*>(dst + kMiscOff), make_int2(s.misc[0], s.misc[1]));
+        __threadfence();
+        st_relaxed_u64(&a.state[i], pack_state(epoch, i == 0 ? kFlagIncl : kFlagAgg, total));
+      }
+    } else {
+      // C. emission item idx: segment idx % split of chunk idx / split
+      const int c_i = (int)(idx / (unsigned)split), seg = (int)(idx % (unsigned)split);
+      const unsigned char* src = spill + (unsigned long long)c_i * P::kSpill;
+      // Every thread waits for the chunk's published state with an acquire load, so its
+      // own reads of the spill slot below are ordered after the slot's stores (no fence
+      // and no barrier before the reload). The waits are bounded; the barrier below
+      // combines them.
+      unsigned long long w = 0;
+      int ok = 0;
+      for (int spins = 0;;) {
+        w = ld_acquire_u64(&a.state[c_i]);
+        if (((unsigned)(w >> 40) & 0xFFFFFFu) == tag && ((w >> 38) & 3ull) != 0ull) {
+          ok = 1;
+          break;
+        }
+        if (++spins > a.spin_limit) break;
+        __nanosleep(spins < 8 ? 32 : 256);
+      }
+      ok = __all_sync(0xffffffffu, ok);  // warp-uniform (warp 0's look-back needs every lane)
+      if (!ok && (t & 31) == 0) atomicOr(&a.ctl->err, ERR_TIMEOUT);
+      // Warp 0 takes the chunk's offset by look-back over the published totals while the
+      // other warps reload the chunk's state (a one-warp CTA does both, in turn).
+      constexpr int TR = T > 32 ? T - 32 : 32;  // reloading threads
+      const int tr = T > 32 ? t - 32 : t;
+      if (t < 32 && ok) {
         const unsigned long long total = __ldcg(
             reinterpret_cast<const uint32_t*>(src + P::kOcc + P::kHalo) + Shape<N>::R);
         // An inclusive state (chunk 0, or a segment of a chunk whose offset another item
@@ -1768,41 +1799,44 @@ k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__
           }
         }
       }
-    }
-    if (ok && tr >= 0) {
-      const int2 m = __ldcg(reinterpret_cast<const int2*>(src + kMiscOff));
-      if (tr == 0) {
-        s.misc[0] = m.x;
-        s.misc[1] = m.y;
+      if (ok && tr >= 0) {
+        const int2 m = __ldcg(reinterpret_cast<const int2*>(src + kMiscOff));
+        if (tr == 0) {
+          s.misc[0] = m.x;
+          s.misc[1] = m.y;
+        }
+        if (m.x > 0) {  // rows with faces: an empty chunk needs no state
+          for (int q = tr; q < kFixed16; q += TR) fixed16[q] = __ldcg(reinterpret_cast<const uint4*>(src) + q);
+          const bool use_list = m.y >= 0;
+          const int elems = use_list ? m.y : m.x * N;
+          const int per = ((elems + split - 1) / split + 31) & ~31;
+          const int lo = min(elems, seg * per), hi = min(elems, lo + per);
+          if (lo < hi) {
+            const int e0 = use_list ? lo : lo / N, e1 = use_list ? hi : (hi - 1) / N + 1;
+            const uint32_t* lsrc = reinterpret_cast<const uint32_t*>(src + (use_list ? kVlOff : kNzOff));
+            uint32_t* ldst = reinterpret_cast<uint32_t*>(use_list ? s.vlist : s.nz);
+            for (int q = (e0 >> 1) + tr; q < (e1 + 1) >> 1; q += TR) ldst[q] = __ldcg(lsrc + q);
+          }
+        }
       }
-      if (m.x > 0) {  // rows with faces: an empty chunk needs no state
-        for (int q = tr; q < kFixed16; q += TR) fixed16[q] = __ldcg(reinterpret_cast<const uint4*>(src) + q);
-        const bool use_list = m.y >= 0;
-        const int elems = use_list ? m.y : m.x * N;
-        const int per = ((elems + split - 1) / split + 31) & ~31;
-        const int lo = min(elems, seg * per), hi = min(elems, lo + per);
-        if (lo < hi) {
-          const int e0 = use_list ? lo : lo / N, e1 = use_list ? hi : (hi - 1) / N + 1;
-          const uint32_t* lsrc = reinterpret_cast<const uint32_t*>(src + (use_list ? kVlOff : kNzOff));
-          uint32_t* ldst = reinterpret_cast<uint32_t*>(use_list ? s.vlist : s.nz);
-          for (int q = (e0 >> 1) + tr; q < (e1 + 1) >> 1; q += TR) ldst[q] = __ldcg(lsrc + q);
+      if (!__syncthreads_and(ok)) break;  // never published (error reported)
+      const int elems = emit_elems(s);
+      const int per = ((elems + split - 1) / split + 31) & ~31;
+      const int lo = min(elems, seg * per), hi = min(elems, lo + per);
+      if (lo < hi) {
+        const vox_chunk_coord c = a.coords[c_i];
+        if (a.stage_faces > 0) {
+          emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch,
+                                a.lane_flush != 0, lo, hi, false);
+          stage_busy = true;
+        } else {
+          emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, lo, hi);
         }
       }
     }
-    if (!__syncthreads_and(ok)) break;  // never published (error reported)
-    const int elems = emit_elems(s);
-    const int per = ((elems + split - 1) / split + 31) & ~31;
-    const int lo = min(elems, seg * per), hi = min(elems, lo + per);
-    if (lo < hi) {
-      const vox_chunk_coord c = a.coords[c_i];
-      if (a.stage_faces > 0)
-        emit_chunk<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, a.stage_faces / kWarpBatch,
-                              a.lane_flush != 0, lo, hi);
-      else emit_chunk_direct<N, LAYOUT>(s, c, s_base, a.cap, a.out0, a.out1, lo, hi);
-    }
-    if (t == 0) s_item = next_item;
+    if (t == 0) s_item = next_tk;
     __syncthreads();
-    k = s_item;
+    tk = s_item;
   }
   if ((t & 31) == 0) bulk_wait_all();  // every lane 0 issued bulk copies
 }

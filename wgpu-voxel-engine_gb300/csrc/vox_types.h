@@ -44,7 +44,7 @@ struct BatchCtl {
   unsigned int bar_count;  // grid barrier: CTAs arrived (reset by the last arriver)
   unsigned int bar_gen;    // grid barrier: generation, advanced by the last arriver
   unsigned int scan_flag;  // phased kernel: the generation whose offset scan is complete
-  unsigned int next2;      // overlap kernel: work-queue ticket of the emission items
+  unsigned int reserved;   // zero
   unsigned int pad;
 };
 
@@ -75,6 +75,7 @@ struct MeshArgs {
   int split;                         // phased kernel: emission segments per chunk
   uint32_t* counts;                  // phased kernel: per-chunk face totals
   int lane_flush;                    // staged faces leave shared memory by plain stores
+  int lag;                           // overlap kernel: generation items ahead of emission
 };
 
 }  // namespace vox
