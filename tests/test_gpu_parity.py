@@ -374,6 +374,70 @@ def test_graph_replay_with_inputs_rewritten_in_place(vox, oracle, schedule):
     ctx.close()
 
 
+@pytest.mark.parametrize("ctas", [0, 1])
+def test_host_entry_point_interleaved_emission(vox, oracle, ctas):
+    """Host outputs with more chunks than two waves of CTAs: the overlap kernel interleaves
+    emission items with generation items (emission two waves behind), and the bytes are
+    the oracle's. One CTA per SM makes the waves short, so most items interleave."""
+    wl = vox.workload("heightmap")
+    cfg = wl.config()
+    coords = vox.grid_coords(range(-20, 20), [0], range(-20, 20))  # 1600 chunks of 16^3
+    n = len(coords)
+    masks = np.asarray(vox.neighbour_masks(coords), np.uint8)
+    w0, w1, woffs = oracle.gen_mesh_batch(cfg, coords, masks)
+    total = int(woffs[-1])
+    ctx = ctx_for(vox, cfg)
+    t = ctx.tuning()
+    ctx.set_tuning(t.threads, t.stage_faces, ctas, vox.SCHEDULE_OVERLAP)
+    hc, hm = Pinned(vox, n * 12), Pinned(vox, n)
+    hc.view(np.int32)[:] = np.asarray(coords, np.int32).reshape(-1)
+    hm.view(np.uint8)[:] = masks
+    h0, h1, ho = Pinned(vox, total * 96), Pinned(vox, total * 24), Pinned(vox, (n + 1) * 8)
+    for rep in range(2):
+        h0.a.fill(0xEE)
+        ctx.gen_mesh_host(hc.ptr, hm.ptr, n, h0.ptr, h1.ptr, total, ho.ptr)
+        assert np.array_equal(ho.view(np.uint64), woffs), rep
+        assert np.array_equal(h0.view(np.uint8), w0), rep
+        assert np.array_equal(h1.view(np.uint8), w1), rep
+    for b in (hc, hm, h0, h1, ho):
+        b.free()
+    ctx.close()
+
+
+@pytest.mark.parametrize("kind", ["height", "density"])
+def test_small_chunks_every_launch_shape(vox, oracle, kind):
+    """8^3 chunks (one- and two-warp CTAs) in every schedule, staging window and CTAs per
+    SM, with fewer chunks than CTAs (emission split into segments) and with more."""
+    cfg = gen_cfg(vox, kind, 8)
+    tried = 0
+    for m in (40, 3000):
+        coords = vox.grid_coords(range(0, 5 if m == 40 else 60), range(0, 1 if m == 40 else 1),
+                                 range(0, 8 if m == 40 else 50))[:m]
+        masks = vox.neighbour_masks(coords)
+        w0, w1, woffs = oracle.gen_mesh_batch(cfg, coords, masks)
+        total = int(woffs[-1])
+        ctx = ctx_for(vox, cfg)
+        d_coords = to_dev(np.asarray(coords, np.int32))
+        d_mask = to_dev(np.asarray(masks, np.uint8))
+        o0, o1 = dev_bytes(max(total, 1) * 96), dev_bytes(max(total, 1) * 24)
+        offs = to_dev(np.zeros(len(coords) + 1, np.uint64))
+        for sched in SCHEDULES:
+            for threads in threads_options(8):
+                for stage in (0, 32, 64):
+                    for cps in (0, 1):
+                        ctx.set_tuning(threads, stage, cps, sched)
+                        o0.fill_(0x5A)
+                        ctx.gen_mesh_batch(d_coords, d_mask, len(coords), o0, o1, total, offs)
+                        ctx.sync()
+                        tag = (m, sched, threads, stage, cps)
+                        assert np.array_equal(to_np(offs), woffs), tag
+                        assert np.array_equal(to_np(o0, total * 96), w0), tag
+                        assert np.array_equal(to_np(o1, total * 24), w1), tag
+                        tried += 1
+        ctx.close()
+    assert tried == 2 * len(SCHEDULES) * 2 * 3 * 2
+
+
 def test_host_entry_point_matches_oracle(vox, oracle):
     wl = vox.workload("plain")
     cfg = wl.config()
