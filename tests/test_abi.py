@@ -28,6 +28,14 @@ def test_header_declares_entry_points():
         assert required in names
 
 
+def test_integration_binding_covers_every_entry_point():
+    """The Rust binding in INTEGRATION.md declares every function of include/*.h."""
+    text = open(os.path.join(REPO, "INTEGRATION.md")).read()
+    bound = set(re.findall(r"pub fn (vox_\w+)\s*\(", text))
+    missing = [n for n in declared_functions() if n not in bound]
+    assert not missing, missing
+
+
 def test_library_exports_every_declared_symbol(vox):
     lib = vox.lib()
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
