@@ -5,8 +5,9 @@
 // masks of a row come from shifts of the row and its neighbours, counts from popc.
 // A deterministic block scan over rows gives every row's first face, the rows that have
 // faces and the voxels that have faces. Chunks of a batch get their global first face
-// either from a decoupled look-back over a device work queue (k_mesh_batch) or from one
-// scan behind a grid barrier (k_mesh_batch_phased). Each warp compacts the faces of a
+// from a decoupled look-back over a device work queue (k_mesh_batch), from one scan
+// behind a grid barrier (k_mesh_batch_phased), or from a look-back over totals published
+// by separate generation items (k_mesh_batch_overlap). Each warp compacts the faces of a
 // run of voxels, stages them 32 at a time in shared memory in their final byte layout,
 // and sends each batch to global memory with a TMA bulk copy
 // (cp.async.bulk.global.shared::cta), or stores them directly.
@@ -101,7 +102,7 @@ struct SmemPlan {
   static constexpr int kMisc = 64;
   static constexpr int kFixed0 = kTables + kOcc + kHalo + kRows + kNz + kVList + kMisc;
   // the chunk state from occ through misc (contiguous in shared memory), as spilled by the
-  // phased kernel: occupancy, halo, row offsets, row and voxel lists, counts
+  // phased and overlap kernels: occupancy, halo, row offsets, row and voxel lists, counts
   static constexpr int kSpill = kOcc + kHalo + kRows + kNz + kVList + kMisc;
   // per-warp face lists (face-parallel emission)
   __host__ __device__ static int list_bytes(int threads) { return (threads / 32) * kWarpFaces * 4; }

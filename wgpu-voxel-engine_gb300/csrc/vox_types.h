@@ -71,8 +71,8 @@ struct MeshArgs {
   int full6;
   int stage_faces;                   // faces per staging window (0: direct global stores)
   int spin_limit;                    // polls before a look-back wait gives up
-  uint32_t* scratch;                 // phased kernel: per-chunk spilled chunk state
-  int split;                         // phased kernel: emission segments per chunk
+  uint32_t* scratch;                 // phased/overlap kernels: per-chunk spilled chunk state
+  int split;                         // phased/overlap kernels: emission segments per chunk
   uint32_t* counts;                  // phased kernel: per-chunk face totals
   int lane_flush;                    // staged faces leave shared memory by plain stores
   int lag;                           // overlap kernel: generation items ahead of emission
