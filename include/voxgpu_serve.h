@@ -51,6 +51,7 @@ typedef struct vox_serve_stats {
   double latency_p99_ms;
   double latency_max_ms;
   double busy_s;               /* wall time between the first request and the last completion */
+  uint64_t cancelled;          /* requests withdrawn by vox_serve_cancel */
 } vox_serve_stats;
 
 typedef struct vox_serve vox_serve;
@@ -85,6 +86,13 @@ int vox_serve_poll(vox_serve* s, uint64_t id, int32_t* state);
  * after timeout_s seconds, VOX_ERR_INVALID for an unknown id, VOX_ERR_OOM if the cache
  * budget cannot hold its batch. */
 int vox_serve_wait(vox_serve* s, uint64_t id, double timeout_s);
+
+/* Withdraws a pending request. A queued chunk leaves the queue; a chunk whose batch is
+ * already on the GPU is discarded when the batch completes (its mesh never becomes
+ * resident). The id becomes VOX_REQ_UNKNOWN. Returns VOX_ERR_INVALID for an unknown id or
+ * a request that is already resident (nothing to withdraw). The reference drops queued
+ * chunks that leave the view the same way (src/chunk_builder.rs:334-352). */
+int vox_serve_cancel(vox_serve* s, uint64_t id);
 
 /* Waits for every batch in flight (and every queued request) and integrates them. */
 int vox_serve_drain(vox_serve* s);

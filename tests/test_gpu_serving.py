@@ -111,3 +111,58 @@ def test_submit_poll_wait_by_request_id(vox, oracle):
     st = server.stats()
     assert st.requested == len(coords) and st.completed == len(coords)
     server.close()
+
+
+def test_cancel_withdraws_queued_and_in_flight_requests(vox, oracle):
+    """A cancelled request never becomes resident, whether it was still queued or its batch
+    was already on the GPU; the other requests complete with their final meshes, and the
+    chunk can be requested again."""
+    wl = vox.workload("heightmap")
+    cfg = wl.config()
+    server = vox.Server(cfg, view_radius=4, max_batch=8, slots=1)
+    coords = [(x, 0, z) for z in range(6) for x in range(6)]
+    ids = server.submit(coords)  # the 8 nearest (to the origin) go to the GPU at once
+    first, far = coords.index((0, 0, 0)), coords.index((5, 0, 5))
+    assert server.cancel(ids[first]) == vox.VOX_OK  # in flight
+    assert server.cancel(ids[far]) == vox.VOX_OK    # queued
+    assert server.cancel(ids[far]) == vox.VOX_ERR_INVALID
+    assert server.cancel(10 ** 9) == vox.VOX_ERR_INVALID
+    server.drain()
+    assert server.poll(ids[first]) == vox.VOX_REQ_UNKNOWN
+    assert server.poll(ids[far]) == vox.VOX_REQ_UNKNOWN
+    assert server.lookup((0, 0, 0)) is None and server.lookup((5, 0, 5)) is None
+    st = server.stats()
+    assert st.cancelled == 2 and st.pending == 0
+    assert st.resident == len(coords) - 2 and st.completed == len(coords) - 2
+    done = coords.index((1, 0, 1))
+    assert server.cancel(ids[done]) == vox.VOX_ERR_INVALID  # resident: nothing to withdraw
+    # requested again: a new id, and the mesh of the chunk alone
+    again = server.submit([(0, 0, 0)])[0]
+    assert again not in ids
+    assert server.wait(again, 30.0) == vox.VOX_OK
+    for c in ((0, 0, 0), (1, 0, 1)):
+        p0, p1, faces = server.lookup(c)
+        w0, w1, woffs = oracle.gen_mesh_batch(cfg, [c], [0x0F])
+        assert faces == int(woffs[-1])
+        assert np.array_equal(fetch(p0, faces * 96), w0)
+        assert np.array_equal(fetch(p1, faces * 24), w1)
+    server.close()
+
+
+def test_cache_budget_exhaustion_reports_oom_and_recovers(vox):
+    """A cache budget below one batch's reservation (an injected allocation failure of the
+    chunk cache): nothing is launched, wait and drain report VOX_ERR_OOM instead of
+    spinning, and withdrawing the requests leaves a usable, empty engine."""
+    wl = vox.workload("heightmap")
+    cfg = wl.config()
+    server = vox.Server(cfg, view_radius=4, max_batch=4, slots=2, cache_budget_bytes=64 << 10)
+    ids = server.submit([(0, 0, 0), (1, 0, 0), (2, 0, 0)])
+    assert server.wait(ids[0], 5.0) == vox.VOX_ERR_OOM
+    with pytest.raises(vox.VoxError):
+        server.drain()
+    for i in ids:
+        assert server.cancel(i) == vox.VOX_OK
+    server.drain()
+    st = server.stats()
+    assert st.launches == 0 and st.pending == 0 and st.resident == 0 and st.cancelled == 3
+    server.close()

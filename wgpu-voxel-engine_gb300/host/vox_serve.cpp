@@ -54,6 +54,8 @@ struct Block {
 
 struct Entry {
   enum State { PENDING, RESIDENT } state = PENDING;
+  bool in_flight = false;  // its batch is on the GPU (a chunk requested again after a
+                           // cancellation waits for its own batch)
   uint64_t id = 0;  // request id (vox_serve_submit / poll / wait)
   double requested_at = 0.0;
   uint64_t last_seen = 0;
@@ -190,6 +192,10 @@ int launch_batch(vox_serve* s, Slot& sl, std::vector<vox_chunk_coord>&& chunks) 
   cudaMemcpyAsync(sl.h_offsets, sl.d_offsets, sizeof(uint64_t) * (m + 1), cudaMemcpyDeviceToHost,
                   sl.stream);
   cudaEventRecord(sl.done, sl.stream);
+  for (const vox_chunk_coord& c : chunks) {
+    auto it = s->entries.find(c);
+    if (it != s->entries.end()) it->second.in_flight = true;
+  }
   sl.chunks = std::move(chunks);
   sl.block = blk;
   sl.cap_faces = cap;
@@ -218,7 +224,7 @@ int integrate(vox_serve* s, Slot& sl, double now) {
   sl.block->refs = m;
   for (int i = 0; i < m; ++i) {
     auto it = s->entries.find(sl.chunks[i]);
-    if (it == s->entries.end()) {  // the request was dropped meanwhile
+    if (it == s->entries.end() || !it->second.in_flight) {  // cancelled meanwhile
       if (--sl.block->refs == 0) {
         s->stats.cache_bytes -= sl.block->bytes;
         free_block(sl.block.get());
@@ -226,6 +232,7 @@ int integrate(vox_serve* s, Slot& sl, double now) {
       continue;
     }
     Entry& e = it->second;
+    e.in_flight = false;
     e.state = Entry::RESIDENT;
     e.block = sl.block;
     e.offset = sl.h_offsets[i];
@@ -468,6 +475,23 @@ int vox_serve_wait(vox_serve* s, uint64_t id, double timeout_s) {
     if (mono_now() >= deadline) return VOX_ERR_TIMEOUT;
     std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
+}
+
+int vox_serve_cancel(vox_serve* s, uint64_t id) {
+  if (!s) return VOX_ERR_INVALID;
+  auto it = s->by_id.find(id);
+  if (it == s->by_id.end()) return VOX_ERR_INVALID;
+  auto e = s->entries.find(it->second);
+  if (e == s->entries.end() || e->second.state != Entry::PENDING) return VOX_ERR_INVALID;
+  // a queued chunk leaves the queue; a launched one is dropped by integrate()
+  auto q = std::find_if(s->queue.begin(), s->queue.end(),
+                        [&](const vox_chunk_coord& c) { return CoordEq()(c, it->second); });
+  if (q != s->queue.end()) s->queue.erase(q);
+  s->entries.erase(e);
+  s->by_id.erase(it);
+  --s->stats.pending;
+  ++s->stats.cancelled;
+  return VOX_OK;
 }
 
 int vox_serve_drain(vox_serve* s) {

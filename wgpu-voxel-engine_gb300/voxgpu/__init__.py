@@ -88,7 +88,7 @@ class ServeStats(ctypes.Structure):
                 ("cache_bytes", ctypes.c_uint64), ("resident", ctypes.c_uint64),
                 ("pending", ctypes.c_uint64), ("latency_p50_ms", ctypes.c_double),
                 ("latency_p99_ms", ctypes.c_double), ("latency_max_ms", ctypes.c_double),
-                ("busy_s", ctypes.c_double)]
+                ("busy_s", ctypes.c_double), ("cancelled", ctypes.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -152,6 +152,7 @@ _SIGS = {
     "vox_serve_submit": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_double, _P]),
     "vox_serve_poll": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_int32)]),
     "vox_serve_wait": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_double]),
+    "vox_serve_cancel": (ctypes.c_int, [_P, ctypes.c_uint64]),
     "vox_serve_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(ServeStats)]),
     "vox_serve_lookup": (ctypes.c_int, [_P, ChunkCoord, ctypes.POINTER(_P), ctypes.POINTER(_P),
                                         ctypes.POINTER(ctypes.c_uint64)]),
@@ -466,6 +467,10 @@ class Server:
     def wait(self, req_id, timeout_s=10.0) -> int:
         """vox_serve_wait; returns the status (VOX_OK when resident)."""
         return self._lib.vox_serve_wait(self._h, req_id, timeout_s)
+
+    def cancel(self, req_id) -> int:
+        """vox_serve_cancel; returns the status (VOX_OK when the request was withdrawn)."""
+        return self._lib.vox_serve_cancel(self._h, req_id)
 
     def stats(self) -> ServeStats:
         s = ServeStats()
