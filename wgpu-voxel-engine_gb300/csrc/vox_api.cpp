@@ -870,8 +870,6 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
     return fail(ctx, VOX_ERR_INVALID, "bad arguments");
   int st = check_outputs(ctx, d_out0, d_out1, cap_faces);
   if (st != VOX_OK) return st;
-  const int N = ctx->cfg.chunk_size;
-  (void)N;
   const int stages[] = {0, kStageSingle, kStageDouble};
   const int ctas[] = {0, 4, 2};
   cudaEvent_t e0, e1;

@@ -346,7 +346,11 @@ int vox_serve_create(const vox_serve_config* cfg, vox_serve** out) {
       cfg->y_max < cfg->y_min || cfg->cache_budget_bytes == 0)
     return VOX_ERR_INVALID;
   *out = nullptr;
-  std::unique_ptr<vox_serve> s(new vox_serve());
+  // a failure below releases whatever was created so far (vox_serve_destroy skips the rest)
+  struct Destroy {
+    void operator()(vox_serve* p) const { vox_serve_destroy(p); }
+  };
+  std::unique_ptr<vox_serve, Destroy> s(new vox_serve());
   s->cfg = *cfg;
   int st = vox_query_sizes(&cfg->chunk, &s->sizes);
   if (st != VOX_OK) return st;
