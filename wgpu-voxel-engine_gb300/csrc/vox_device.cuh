@@ -27,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include "voxgpu.h"
+#include "vox_schedule.h"
 #include "vox_types.h"
 
 namespace vox {
@@ -1744,24 +1745,6 @@ k_mesh_batch_phased(const __grid_constant__ MeshArgs a, const __grid_constant__ 
 // a normal launch. L = n (all generation first) suits launches bound by issue; a smaller L
 // starts emission early, which hides generation behind a slow output (host memory).
 // ------------------------------------------------------------------------------------
-
-// Item of ticket t: returns 0 (generation, idx = chunk), 1 (emission, idx = item) or 2
-// (past the end). n chunks, `items` emission items (>= n), lag L in [0, n].
-__device__ __forceinline__ int overlap_ticket(unsigned t, unsigned n, unsigned items, unsigned L,
-                                              unsigned& idx) {
-  if (t < L) {
-    idx = t;
-    return 0;
-  }
-  const unsigned P = n - L;  // interleaved pairs
-  const unsigned u = t - L;
-  if (u < 2u * P) {
-    idx = (u & 1u) ? (u >> 1) : L + (u >> 1);
-    return (u & 1u) ? 1 : 0;
-  }
-  idx = P + (u - 2u * P);
-  return idx < items ? 1 : 2;
-}
 
 template <int N, int GM, int LAYOUT, int T>
 __global__ void __launch_bounds__(T)
