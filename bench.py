@@ -275,7 +275,9 @@ def run_reference(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD_TEXT[args.workload], "chunks_per_step": sample},
+        "config": {"workload": WORKLOAD_TEXT[args.workload], "chunks": len(coords),
+                   "chunk_size": cfg.chunk_size, "layout": args.layout,
+                   "chunks_per_step": sample},
         "cpu_baseline": {"value": value, "unit": "chunks/s", "cores": threads, "kind": "port",
                          "sample": f"passes over {sample} of {len(coords)} chunks for about "
                                    f"{window:.1f} s per step; the reference is Rust (no toolchain "

@@ -1,0 +1,28 @@
+"""bench.py --impl reference runs on the host cores alone (no GPU) and prints one JSON line
+with the contract's keys, on the same workload, metric and unit as the GPU arm."""
+import json
+import os
+import subprocess
+import sys
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_reference_arm_prints_one_contract_line(built):
+    r = subprocess.run([sys.executable, os.path.join(REPO, "bench.py"), "--impl", "reference",
+                        "--steps", "1", "--warmup", "0"],
+                       capture_output=True, text=True, timeout=300, cwd=REPO)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    sys.path.insert(0, REPO)
+    import bench
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC
+    assert d["unit"] == "chunks/s" and d["higher_is_better"] is True and d["value"] > 0
+    assert d["config"]["workload"] == bench.WORKLOAD_TEXT["heightmap"]
+    assert d["config"]["chunks"] == 1024 and d["config"]["chunk_size"] == 16
+    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["cores"] >= 1
+    assert d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"] == {"value": d["value"], "unit": "chunks/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
