@@ -54,6 +54,8 @@ struct vox_ctx {
   TablesDev h_tables{};  // the fused batch kernels take the tables as a kernel parameter
   BatchCtl* d_ctl = nullptr;
   BatchCtl* h_ctl = nullptr;  // pinned
+  unsigned* h_err_mirror = nullptr;  // page-locked, mapped: status of host-output launches
+  unsigned* d_err_mirror = nullptr;  // its device address
   unsigned long long* d_state = nullptr;
   size_t state_cap = 0;
   unsigned long long launches = 0;
@@ -454,6 +456,10 @@ int vox_ctx_create(const vox_config* cfg, void* stream, vox_ctx** out) {
   if (cudaMalloc(&ctx->d_ctl, sizeof(BatchCtl)) != cudaSuccess) return cleanup(VOX_ERR_OOM);
   if (cudaMemset(ctx->d_ctl, 0, sizeof(BatchCtl)) != cudaSuccess) return cleanup(VOX_ERR_CUDA);
   if (cudaMallocHost(&ctx->h_ctl, sizeof(BatchCtl)) != cudaSuccess) return cleanup(VOX_ERR_OOM);
+  if (cudaHostAlloc(&ctx->h_err_mirror, sizeof(unsigned), cudaHostAllocMapped) != cudaSuccess ||
+      cudaHostGetDevicePointer(&ctx->d_err_mirror, ctx->h_err_mirror, 0) != cudaSuccess)
+    return cleanup(VOX_ERR_OOM);
+  *ctx->h_err_mirror = 0u;
   // Every meshing kernel may use up to the full shared memory of an SM; the tuning
   // decides how much a launch actually takes.
   const int layout = cfg->layout;
@@ -492,6 +498,7 @@ int vox_ctx_destroy(vox_ctx* ctx) {
   cudaFree(ctx->d_out0);
   cudaFree(ctx->d_out1);
   if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
+  if (ctx->h_err_mirror) cudaFreeHost(ctx->h_err_mirror);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return VOX_OK;
@@ -524,6 +531,17 @@ static int sync_locked(vox_ctx* ctx) {
   if (err & ERR_TIMEOUT) return fail(ctx, VOX_ERR_TIMEOUT, "a device-side wait gave up");
   if (err & ERR_BAD_INPUT) return fail(ctx, VOX_ERR_INVALID, "a slot index was out of range");
   return fail(ctx, VOX_ERR_CAPACITY, "output capacity exceeded");
+}
+
+// sync_locked for a launch that mirrored its status into ctx->h_err_mirror: the stream
+// sync alone, then the mirrored word (it holds the error bits of every launch so far); the
+// copy path of sync_locked only when there is an error to clear or no mirrored value.
+static int sync_mirrored(vox_ctx* ctx) {
+  VOX_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
+  const unsigned m = *reinterpret_cast<volatile unsigned*>(ctx->h_err_mirror);
+  *ctx->h_err_mirror = 0u;
+  if (m == kMirrorValid) return VOX_OK;
+  return sync_locked(ctx);
 }
 
 int vox_ctx_sync(vox_ctx* ctx) {
@@ -710,8 +728,15 @@ int vox_gen_mesh_host(vox_ctx* ctx, const vox_chunk_coord* h_coords, const uint8
       a.out1 = z1;
       a.cap = cap_faces;
       a.face_offsets = static_cast<unsigned long long*>(zoff);
+      // the kernel flags a capacity overflow in the error word; the look-back and overlap
+      // kernels also mirror that word into page-locked memory at their end
+      const bool mirror = ctx->schedule != VOX_SCHEDULE_PHASED;
+      if (mirror) {
+        *ctx->h_err_mirror = 0u;
+        a.err_mirror = ctx->d_err_mirror;
+      }
       if ((st = batch_launch(ctx, a, ctx->gm, true)) != VOX_OK) return st;
-      return sync_locked(ctx);  // the kernel flags a capacity overflow in the error word
+      return mirror ? sync_mirrored(ctx) : sync_locked(ctx);
     }
   }
   if ((st = grow(ctx, &ctx->d_in, &ctx->in_cap, in_bytes, "cudaMalloc(inputs)")) != VOX_OK) return st;

@@ -1005,6 +1005,24 @@ static __device__ unsigned long long lookback(unsigned long long* state, BatchCt
   return excl;
 }
 
+// Status mirror of a launch whose caller waits for it (outputs in host memory): the last
+// CTA to finish copies the error word, with kMirrorValid set, into a page-locked host word,
+// so that the host reads the status after the stream sync without a device-to-host copy.
+// Every earlier launch on the stream has completed, so the word holds their bits too.
+__device__ __forceinline__ void finish_launch(const MeshArgs& a) {
+  if (a.err_mirror == nullptr) return;
+  __syncthreads();  // this CTA's error bits are set
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(&a.ctl->done, 1u) == gridDim.x - 1u) {
+      __threadfence();
+      const unsigned e = atomicOr(&a.ctl->err, 0u);
+      a.ctl->done = 0u;
+      *reinterpret_cast<volatile unsigned*>(a.err_mirror) = e | kMirrorValid;
+    }
+  }
+}
+
 // Staging-buffer placement of window records. The index records (vertex layout) and the
 // instance records are shifted so that the bulk-copied part starts on a 16-byte boundary
 // in shared and in global memory (global face g0 + l0 with (g0 + l0) even, resp. a
@@ -1493,6 +1511,7 @@ k_mesh_batch(const __grid_constant__ MeshArgs a, const __grid_constant__ TablesD
     i = s_item;
   }
   if ((threadIdx.x & 31) == 0) bulk_wait_all();  // every lane 0 issued bulk copies
+  finish_launch(a);
 }
 
 // ------------------------------------------------------------------------------------
@@ -1907,6 +1926,7 @@ k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__
     tk = s_item;
   }
   if ((t & 31) == 0) bulk_wait_all();  // every lane 0 issued bulk copies
+  finish_launch(a);
 }
 
 // Plain per-chunk mesher: one chunk, one CTA, one launch (no queue, no look-back).

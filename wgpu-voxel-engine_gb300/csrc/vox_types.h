@@ -11,6 +11,8 @@ namespace vox {
 constexpr unsigned ERR_TIMEOUT = 1u;   // a look-back wait gave up
 constexpr unsigned ERR_CAPACITY = 2u;  // output capacity exceeded
 constexpr unsigned ERR_BAD_INPUT = 4u; // a slot index out of range
+// set in a status mirror word by the launch that wrote it (MeshArgs::err_mirror)
+constexpr unsigned kMirrorValid = 0x80000000u;
 
 // Bounded spin: ~2^22 polls with a growing nanosleep (well under 2 s in total).
 constexpr int kSpinLimit = 1 << 22;
@@ -44,7 +46,7 @@ struct BatchCtl {
   unsigned int bar_count;  // grid barrier: CTAs arrived (reset by the last arriver)
   unsigned int bar_gen;    // grid barrier: generation, advanced by the last arriver
   unsigned int scan_flag;  // phased kernel: the generation whose offset scan is complete
-  unsigned int reserved;   // zero
+  unsigned int done;       // CTAs finished in a launch that mirrors its status (reset by the last)
   unsigned int pad;
 };
 
@@ -76,6 +78,7 @@ struct MeshArgs {
   uint32_t* counts;                  // phased kernel: per-chunk face totals
   int lane_flush;                    // staged faces leave shared memory by plain stores
   int lag;                           // overlap kernel: generation items ahead of emission
+  unsigned* err_mirror;              // page-locked host word for the launch's status, or null
 };
 
 }  // namespace vox
