@@ -16,6 +16,7 @@
 #include "voxgpu.h"
 #include "vox_kernels.h"
 #include "vox_tables.h"
+#include "vox_trace.h"
 #include "vox_types.h"
 
 using namespace vox;
@@ -545,6 +546,7 @@ static int sync_mirrored(vox_ctx* ctx) {
 }
 
 int vox_ctx_sync(vox_ctx* ctx) {
+  vox::TraceRange trace_("vox_ctx_sync");
   if (!ctx) return VOX_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->mu);
   return sync_locked(ctx);
@@ -552,6 +554,7 @@ int vox_ctx_sync(vox_ctx* ctx) {
 
 int vox_generate(vox_ctx* ctx, const vox_chunk_coord* d_coords, int32_t n,
                  int64_t chunk_index_base, uint32_t* d_occ) {
+  vox::TraceRange trace_("vox_generate");
   if (!ctx) return VOX_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (n < 0 || (n > 0 && (!d_coords || !d_occ))) return fail(ctx, VOX_ERR_INVALID, "bad arguments");
@@ -567,6 +570,7 @@ int vox_generate(vox_ctx* ctx, const vox_chunk_coord* d_coords, int32_t n,
 }
 
 int vox_occ_to_cubes(vox_ctx* ctx, const uint32_t* d_occ, int32_t n, uint8_t* d_cubes) {
+  vox::TraceRange trace_("vox_occ_to_cubes");
   if (!ctx) return VOX_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (n < 0 || (n > 0 && (!d_occ || !d_cubes))) return fail(ctx, VOX_ERR_INVALID, "bad arguments");
@@ -576,6 +580,7 @@ int vox_occ_to_cubes(vox_ctx* ctx, const uint32_t* d_occ, int32_t n, uint8_t* d_
 }
 
 int vox_cubes_to_occ(vox_ctx* ctx, const uint8_t* d_cubes, int32_t n, uint32_t* d_occ) {
+  vox::TraceRange trace_("vox_cubes_to_occ");
   if (!ctx) return VOX_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (n < 0 || (n > 0 && (!d_occ || !d_cubes))) return fail(ctx, VOX_ERR_INVALID, "bad arguments");
@@ -587,6 +592,7 @@ int vox_cubes_to_occ(vox_ctx* ctx, const uint8_t* d_cubes, int32_t n, uint32_t* 
 int vox_mesh(vox_ctx* ctx, const uint32_t* d_occ, const uint32_t* const d_nbr[6],
              vox_chunk_coord coord, void* d_out0, void* d_out1, uint64_t cap_faces,
              uint64_t* d_face_count) {
+  vox::TraceRange trace_("vox_mesh");
   if (!ctx) return VOX_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (!d_occ || !d_face_count) return fail(ctx, VOX_ERR_INVALID, "d_occ and d_face_count are required");
@@ -612,6 +618,7 @@ int vox_mesh_batch(vox_ctx* ctx, const uint32_t* d_occ_pool, int32_t pool_slots,
                    const int32_t* d_slots, const int32_t* d_nbr_slots,
                    const vox_chunk_coord* d_coords, int32_t n, void* d_out0, void* d_out1,
                    uint64_t cap_faces, uint64_t* d_face_offsets) {
+  vox::TraceRange trace_("vox_mesh_batch");
   if (!ctx) return VOX_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (n < 0 || (n > 0 && (!d_occ_pool || !d_slots || !d_coords || !d_face_offsets)) ||
@@ -637,6 +644,7 @@ int vox_mesh_batch(vox_ctx* ctx, const uint32_t* d_occ_pool, int32_t pool_slots,
 int vox_gen_mesh_batch(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
                        int32_t n, int64_t chunk_index_base, void* d_out0, void* d_out1,
                        uint64_t cap_faces, uint64_t* d_face_offsets) {
+  vox::TraceRange trace_("vox_gen_mesh_batch");
   if (!ctx) return VOX_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (n < 0 || (n > 0 && (!d_coords || !d_face_offsets)))
@@ -681,6 +689,7 @@ static void* mapped_host(const void* h) {
 int vox_gen_mesh_host(vox_ctx* ctx, const vox_chunk_coord* h_coords, const uint8_t* h_nbr_mask,
                       int32_t n, int64_t chunk_index_base, void* h_out0, void* h_out1,
                       uint64_t cap_faces, uint64_t* h_face_offsets) {
+  vox::TraceRange trace_("vox_gen_mesh_host");
   if (!ctx) return VOX_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (n < 0 || (n > 0 && (!h_coords || !h_face_offsets)))
@@ -814,6 +823,7 @@ int vox_frustum_planes(const float m[16], float planes[24]) {
 
 int vox_frustum_cull(vox_ctx* ctx, const float planes[24], const vox_chunk_coord* d_coords,
                      int32_t n, uint8_t* d_visible) {
+  vox::TraceRange trace_("vox_frustum_cull");
   if (!ctx) return VOX_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (!planes || n < 0 || (n > 0 && (!d_coords || !d_visible)))
@@ -828,6 +838,7 @@ int vox_frustum_cull(vox_ctx* ctx, const float planes[24], const vox_chunk_coord
 int vox_draw_list(vox_ctx* ctx, const float planes[24], const vox_chunk_coord* d_coords,
                   const uint64_t* d_face_offsets, int32_t n, vox_draw_indexed_indirect* d_draws,
                   uint32_t* d_count) {
+  vox::TraceRange trace_("vox_draw_list");
   if (!ctx) return VOX_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (!planes || !d_count || n < 0 || (n > 0 && (!d_coords || !d_face_offsets || !d_draws)))
@@ -844,6 +855,7 @@ int vox_draw_list(vox_ctx* ctx, const float planes[24], const vox_chunk_coord* d
 int vox_raster(vox_ctx* ctx, const float view_proj_colmajor[16], const void* d_vertices,
                const void* d_indices, uint64_t faces, int32_t width, int32_t height,
                uint64_t* d_depth_keys, uint8_t* d_rgba) {
+  vox::TraceRange trace_("vox_raster");
   if (!ctx) return VOX_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (ctx->cfg.layout != VOX_LAYOUT_VERTEX)
@@ -889,6 +901,7 @@ int vox_ctx_set_tuning(vox_ctx* ctx, const vox_tuning* t) {
 int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
                  int32_t n, int64_t chunk_index_base, void* d_out0, void* d_out1,
                  uint64_t cap_faces, uint64_t* d_face_offsets, int32_t iters, vox_tuning* out) {
+  vox::TraceRange trace_("vox_autotune");
   if (!ctx) return VOX_ERR_INVALID;
   std::lock_guard<std::mutex> lk(ctx->mu);
   if (n <= 0 || !d_coords || !d_face_offsets || iters < 1)
@@ -994,6 +1007,7 @@ static void graph_free(vox_graph* g) {
 int vox_graph_capture(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
                       int32_t n, int64_t chunk_index_base, void* d_out0, void* d_out1,
                       uint64_t cap_faces, uint64_t* d_face_offsets, vox_graph** out) {
+  vox::TraceRange trace_("vox_graph_capture");
   if (!ctx || !out) return VOX_ERR_INVALID;
   *out = nullptr;
   std::lock_guard<std::mutex> lk(ctx->mu);
@@ -1058,6 +1072,7 @@ int vox_graph_capture(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8
 }
 
 int vox_graph_launch(vox_graph* g) {
+  vox::TraceRange trace_("vox_graph_launch");
   if (!g || !g->ctx) return VOX_ERR_INVALID;
   vox_ctx* ctx = g->ctx;
   std::lock_guard<std::mutex> lk(ctx->mu);

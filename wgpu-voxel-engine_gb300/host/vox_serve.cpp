@@ -21,6 +21,7 @@
 
 #include "voxgpu.h"
 #include "voxgpu_serve.h"
+#include "../csrc/vox_trace.h"
 
 namespace {
 
@@ -414,6 +415,7 @@ int vox_serve_destroy(vox_serve* s) {
 double vox_serve_now(void) { return mono_now(); }
 
 int vox_serve_frame(vox_serve* s, const float view_proj[16], const float eye[3], double now_s) {
+  vox::TraceRange trace_("vox_serve_frame");
   if (!s || !view_proj || !eye) return VOX_ERR_INVALID;
   if (now_s < 0.0) now_s = mono_now();
   ++s->frame;
@@ -439,6 +441,7 @@ int vox_serve_frame(vox_serve* s, const float view_proj[16], const float eye[3],
 
 int vox_serve_submit(vox_serve* s, const vox_chunk_coord* coords, int32_t n, double now_s,
                      uint64_t* ids_out) {
+  vox::TraceRange trace_("vox_serve_submit");
   if (!s || n < 0 || (n > 0 && !coords)) return VOX_ERR_INVALID;
   if (now_s < 0.0) now_s = mono_now();
   for (int32_t i = 0; i < n; ++i) {
@@ -457,6 +460,7 @@ static int32_t request_state(vox_serve* s, uint64_t id) {
 }
 
 int vox_serve_poll(vox_serve* s, uint64_t id, int32_t* state) {
+  vox::TraceRange trace_("vox_serve_poll");
   if (!s || !state) return VOX_ERR_INVALID;
   const int st = poll_and_admit(s, false);
   if (st != VOX_OK) return st;
@@ -465,6 +469,7 @@ int vox_serve_poll(vox_serve* s, uint64_t id, int32_t* state) {
 }
 
 int vox_serve_wait(vox_serve* s, uint64_t id, double timeout_s) {
+  vox::TraceRange trace_("vox_serve_wait");
   if (!s) return VOX_ERR_INVALID;
   const double deadline = mono_now() + timeout_s;
   for (;;) {
@@ -482,6 +487,7 @@ int vox_serve_wait(vox_serve* s, uint64_t id, double timeout_s) {
 }
 
 int vox_serve_cancel(vox_serve* s, uint64_t id) {
+  vox::TraceRange trace_("vox_serve_cancel");
   if (!s) return VOX_ERR_INVALID;
   auto it = s->by_id.find(id);
   if (it == s->by_id.end()) return VOX_ERR_INVALID;
@@ -499,6 +505,7 @@ int vox_serve_cancel(vox_serve* s, uint64_t id) {
 }
 
 int vox_serve_drain(vox_serve* s) {
+  vox::TraceRange trace_("vox_serve_drain");
   if (!s) return VOX_ERR_INVALID;
   for (;;) {
     bool busy = false;

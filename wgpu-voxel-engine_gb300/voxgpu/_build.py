@@ -104,7 +104,7 @@ def build_library(verbose: bool = False, extra_nvcc=None) -> str:
                     print(out)
     if jobs or not _stamp_ok(LIB_PATH) or os.path.getmtime(LIB_PATH) < _newest(objs):
         tmp = LIB_PATH + ".tmp"
-        _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread"])
+        _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lpthread", "-ldl"])
         os.replace(tmp, LIB_PATH)
         _write_stamp(LIB_PATH)
     return LIB_PATH
