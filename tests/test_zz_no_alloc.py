@@ -86,3 +86,76 @@ def test_noalloc_reports_a_short_output(vox):
     st = _noalloc(vox, cfg, d_coords, d_mask, 8, o0, o1, 100, offs)
     assert st == vox.VOX_ERR_CAPACITY
     assert int(to_np(offs)[8]) > 100  # the required size is still returned
+
+
+def test_noalloc_full_state_array(vox):
+    """A call of exactly 16384 chunks uses every look-back state of the static array: the
+    face offsets must equal the context entry point's (8^3 chunks, no output written)."""
+    cfg = vox.make_config(chunk_size=8, octaves=1, seed=42, frequency=1 / 64, amplitude=12.0,
+                          base_height=4.0)
+    n = 16384
+    coords = vox.grid_coords(range(-64, 64), range(-1, 1), range(-64, 0))
+    assert len(coords) == n
+    d_coords = to_dev(np.asarray(coords, np.int32))
+    ctx = ctx_for(vox, cfg)
+    roffs = to_dev(np.zeros(n + 1, np.uint64))
+    ctx.gen_mesh_batch(d_coords, None, n, None, None, 0, roffs)
+    assert ctx.sync(raise_on_error=False) == vox.VOX_ERR_CAPACITY  # nothing fits in 0 faces
+    want = to_np(roffs)
+    ctx.close()
+    assert int(want[n]) > 0
+    for call in range(2):
+        offs = to_dev(np.zeros(n + 1, np.uint64))
+        st = _noalloc_raw(vox, cfg, d_coords.data_ptr(), None, n, None, None, 0, offs.data_ptr())
+        assert st == vox.VOX_ERR_CAPACITY, (call, st)
+        assert np.array_equal(to_np(offs), want), call
+
+
+def _noalloc_raw(vox, cfg, coords, mask, n, out0, out1, cap, offs, stream=None):
+    import torch
+    if stream is None:
+        stream = torch.cuda.current_stream().cuda_stream
+    return vox.lib().vox_gen_mesh_batch_noalloc(ctypes.byref(cfg), ctypes.c_void_p(stream),
+                                                coords, mask, n, 0, out0, out1, cap, offs)
+
+
+def test_noalloc_rejects_misaligned_or_missing_outputs(vox):
+    cfg = vox.workload("plain").config()
+    d_coords = to_dev(np.zeros((4, 3), np.int32))
+    o = dev_bytes(1 << 16)
+    offs = to_dev(np.zeros(5, np.uint64))
+    p = o.data_ptr()
+    assert _noalloc_raw(vox, cfg, d_coords.data_ptr(), None, 4, p + 4, p, 8, offs.data_ptr()) \
+        == vox.VOX_ERR_INVALID
+    assert _noalloc_raw(vox, cfg, d_coords.data_ptr(), None, 4, p, p + 8, 8, offs.data_ptr()) \
+        == vox.VOX_ERR_INVALID
+    assert _noalloc_raw(vox, cfg, d_coords.data_ptr(), None, 4, None, p, 8, offs.data_ptr()) \
+        == vox.VOX_ERR_INVALID
+    assert _noalloc_raw(vox, cfg, d_coords.data_ptr(), None, 4, p, None, 8, offs.data_ptr()) \
+        == vox.VOX_ERR_INVALID
+
+
+def test_noalloc_refuses_a_capturing_stream(vox):
+    """The call is synchronous: on a stream under capture it returns VOX_ERR_INVALID and
+    queues nothing, and the capture stays valid."""
+    import torch
+    cfg = vox.workload("plain").config()
+    d_coords = to_dev(np.zeros((4, 3), np.int32))
+    o0, o1 = dev_bytes(1 << 16), dev_bytes(1 << 16)
+    offs = to_dev(np.zeros(5, np.uint64))
+    marker = torch.zeros(4, dtype=torch.float32, device="cuda")
+    side = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(side):
+        g.capture_begin()
+        try:
+            st = _noalloc_raw(vox, cfg, d_coords.data_ptr(), None, 4, o0.data_ptr(),
+                              o1.data_ptr(), 8, offs.data_ptr(), stream=side.cuda_stream)
+            marker.add_(1.0)  # the capture keeps one node of its own
+        finally:
+            g.capture_end()
+    assert st == vox.VOX_ERR_INVALID
+    g.replay()
+    torch.cuda.synchronize()
+    assert marker.cpu().tolist() == [1.0] * 4

@@ -11,10 +11,14 @@
 // holds it (about 129 KiB) until the process exits.
 //
 // Set-up: the first call on a device looks up the array's device address with
-// cudaGetSymbolAddress (with that device current) and caches it; make that first call
-// before any stream capture. Every call shares the array and it keeps the last call's
-// contents: each call clears the queue ticket and the error word before its launch, and
-// calls whose work overlaps on the GPU race on the shared array.
+// cudaGetSymbolAddress (with that device current) and caches it for the life of the
+// process; do not use this entry point across cudaDeviceReset, which reloads the module and
+// leaves the cached address stale. Every call is synchronous (it reads the launch's status
+// back and waits for the stream), so no call may be made on a stream that is being
+// captured: such a call returns VOX_ERR_INVALID before it touches the GPU. Every call
+// shares the array and it keeps the last call's contents: each call clears the queue
+// ticket and the error word before its launch, and calls whose work overlaps on the GPU
+// race on the shared array.
 #include <cuda_runtime.h>
 
 #include <cstddef>
@@ -160,6 +164,15 @@ extern "C" int vox_gen_mesh_batch_noalloc(const vox_config* cfg, void* stream,
     return noalloc_fail(VOX_ERR_NO_DEVICE, "no current CUDA device");
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // The call reads its status back and synchronises the stream, which a stream capture
+  // does not allow: refuse a capturing stream before any work is queued on it.
+  cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap_status) != cudaSuccess) {
+    cudaGetLastError();
+    return noalloc_fail(VOX_ERR_CUDA, "cudaStreamIsCapturing failed");
+  }
+  if (cap_status != cudaStreamCaptureStatusNone)
+    return noalloc_fail(VOX_ERR_INVALID, "the call is synchronous and cannot run on a capturing stream");
   const int N = cfg->chunk_size;
   const int gm = cfg->gen.kind == VOX_GEN_HEIGHTMAP ? GM_HEIGHT
                : cfg->gen.kind == VOX_GEN_DENSITY   ? GM_DENSITY
@@ -187,8 +200,10 @@ extern "C" int vox_gen_mesh_batch_noalloc(const vox_config* cfg, void* stream,
       g_scratch_ptr[dev] = static_cast<NoAllocScratch*>(p);
     }
     scratch = g_scratch_ptr[dev];
-    // Look-back states carry a 24-bit launch epoch; wipe them before a tag can repeat.
-    if (g_launches[dev] > 0 && (g_launches[dev] & ((1ull << 23) - 1)) == 0 &&
+    // Look-back states carry a 24-bit launch epoch, which every launch advances by one (its
+    // last work ticket is always drawn); wipe them every 2^22 calls, well before a tag can
+    // repeat.
+    if (g_launches[dev] > 0 && (g_launches[dev] & ((1ull << 22) - 1)) == 0 &&
         cudaMemsetAsync(scratch->state, 0, sizeof(scratch->state), st) != cudaSuccess)
       return noalloc_fail(VOX_ERR_CUDA, "cudaMemsetAsync(state) failed");
     ++g_launches[dev];
@@ -247,18 +262,10 @@ extern "C" int vox_gen_mesh_batch_noalloc(const vox_config* cfg, void* stream,
     return VOX_ERR_CUDA;
   }
   const unsigned err = ctl.err;
-  if (err & ERR_TIMEOUT) {
-    // a fresh look-back epoch: no state word of the failed launch can match a later tag
-    ctl.epoch += 1;
-    if (cudaMemcpyAsync(&scratch->ctl.epoch, &ctl.epoch, sizeof ctl.epoch, cudaMemcpyHostToDevice,
-                        st) != cudaSuccess ||
-        cudaStreamSynchronize(st) != cudaSuccess) {
-      const cudaError_t e = cudaGetLastError();
-      std::fprintf(stderr, "voxgpu: %s\n", cudaGetErrorString(e));
-      return VOX_ERR_CUDA;
-    }
-    return VOX_ERR_TIMEOUT;
-  }
+  // A timed-out wait does not stop the kernel from drawing every ticket, so its last
+  // ticket has already reset the queue and advanced the epoch: no state word of the
+  // failed launch can match a later launch's tag.
+  if (err & ERR_TIMEOUT) return VOX_ERR_TIMEOUT;
   if (err & ERR_CAPACITY) return VOX_ERR_CAPACITY;
   return VOX_OK;
 }
