@@ -689,6 +689,223 @@ int64_t or_baseline_run(const vox_config* cfg, const vox_chunk_coord* coords,
 }
 
 /* ------------------------------------------------------------------------------------ */
+/* Per-chunk digests of whole batches (parity at full workload sizes)                    */
+/* ------------------------------------------------------------------------------------ */
+
+static uint64_t or_mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+uint64_t or_digest(const void* bytes, uint64_t len) {
+  const uint8_t* b = (const uint8_t*)bytes;
+  uint64_t h = len;
+  uint64_t k = 0;
+  for (uint64_t off = 0; off < len; off += 8, ++k) {
+    uint64_t w = 0;
+    const uint64_t m = len - off < 8 ? len - off : 8;
+    for (uint64_t j = 0; j < m; ++j) w |= (uint64_t)b[off + j] << (8 * j);
+    h = or_mix64(h ^ or_mix64(w + k * 0x9E3779B97F4A7C15ULL));
+  }
+  return h;
+}
+
+typedef struct {
+  const void* out0;
+  const void* out1;
+  const uint64_t* offs;
+  int32_t n;
+  int32_t b0, b1;
+  uint64_t* digests;
+  volatile int64_t next;
+} digest_job;
+
+static void* digest_worker(void* arg) {
+  digest_job* j = (digest_job*)arg;
+  for (;;) {
+    const int64_t i = __atomic_fetch_add(&j->next, 1, __ATOMIC_RELAXED);
+    if (i >= j->n) break;
+    const uint64_t lo = j->offs[i], hi = j->offs[i + 1];
+    j->digests[2 * i] = or_digest((const uint8_t*)j->out0 + lo * (uint64_t)j->b0, (hi - lo) * (uint64_t)j->b0);
+    j->digests[2 * i + 1] =
+        j->b1 > 0 ? or_digest((const uint8_t*)j->out1 + lo * (uint64_t)j->b1, (hi - lo) * (uint64_t)j->b1)
+                  : 0;
+  }
+  return NULL;
+}
+
+void or_chunk_digests(const void* out0, const void* out1, const uint64_t* offs, int32_t n,
+                      int32_t b0, int32_t b1, int nthreads, uint64_t* digests) {
+  digest_job j;
+  memset(&j, 0, sizeof j);
+  j.out0 = out0;
+  j.out1 = out1;
+  j.offs = offs;
+  j.n = n;
+  j.b0 = b0;
+  j.b1 = b1;
+  j.digests = digests;
+  if (nthreads < 1) nthreads = 1;
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+  if (!th) {
+    digest_worker(&j);
+    return;
+  }
+  for (int t = 0; t < nthreads; ++t) pthread_create(&th[t], NULL, digest_worker, &j);
+  for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+  free(th);
+}
+
+typedef struct {
+  const vox_config* cfg;
+  const vox_chunk_coord* coords;
+  const uint8_t* nbr_mask;
+  int32_t n;
+  int64_t index_base;
+  uint64_t* counts;
+  uint64_t* digests;
+  volatile int64_t next;
+  volatile int failed;
+} gen_digest_job;
+
+/* One chunk of or_gen_mesh_batch (the same generation, neighbour halo and emission), its
+ * faces emitted into the worker's own buffers. */
+static void* gen_digest_worker(void* arg) {
+  gen_digest_job* j = (gen_digest_job*)arg;
+  const vox_config* cfg = j->cfg;
+  const int N = cfg->chunk_size;
+  const size_t vox = (size_t)N * N * N;
+  uint8_t* cubes = (uint8_t*)malloc(vox * 7);
+  const size_t max_faces = (size_t)3 * vox + (size_t)6 * N * N;
+  or_face* faces = j->digests ? (or_face*)malloc(sizeof(or_face) * max_faces) : NULL;
+  const size_t b0 = cfg->layout == VOX_LAYOUT_INSTANCED ? sizeof(vox_instance_raw) : 4 * sizeof(vox_vertex);
+  const size_t b1 = cfg->layout == VOX_LAYOUT_INSTANCED ? 0 : 6 * sizeof(uint32_t);
+  uint8_t* o0 = j->digests ? (uint8_t*)malloc(b0 * max_faces) : NULL;
+  uint8_t* o1 = j->digests && b1 ? (uint8_t*)malloc(b1 * max_faces) : NULL;
+  if (!cubes || (j->digests && (!faces || !o0 || (b1 && !o1)))) {
+    j->failed = 1;
+    free(cubes);
+    free(faces);
+    free(o0);
+    free(o1);
+    return NULL;
+  }
+  for (;;) {
+    const int64_t i = __atomic_fetch_add(&j->next, 1, __ATOMIC_RELAXED);
+    if (i >= j->n) break;
+    or_generate_cubes(cfg, j->coords[i], j->index_base + i, cubes);
+    const uint8_t* adj[6] = {0, 0, 0, 0, 0, 0};
+    uint8_t m = j->nbr_mask ? j->nbr_mask[i] : 0;
+    if (cfg->gen.kind == VOX_GEN_BERNOULLI) m = 0; /* Bernoulli chunks are isolated */
+    for (int d = 0; d < 6; ++d) {
+      if (!((m >> d) & 1)) continue;
+      if (d >= 4 && cfg->cull_mode != VOX_CULL_FULL6) continue;
+      uint8_t* nb = cubes + vox * (size_t)(1 + d);
+      or_generate_cubes(cfg, nbr_coord(j->coords[i], d), 0, nb);
+      adj[d] = nb;
+    }
+    const int64_t cnt = or_cull_faces(N, cfg->cull_mode, cubes, adj, faces, faces ? (int64_t)max_faces : 0);
+    j->counts[i] = (uint64_t)cnt;
+    if (j->digests) {
+      emit_faces(cfg, j->coords[i], faces, cnt, 0, o0, o1);
+      j->digests[2 * i] = or_digest(o0, (uint64_t)cnt * b0);
+      j->digests[2 * i + 1] = b1 ? or_digest(o1, (uint64_t)cnt * b1) : 0;
+    }
+  }
+  free(cubes);
+  free(faces);
+  free(o0);
+  free(o1);
+  return NULL;
+}
+
+int or_gen_mesh_digests(const vox_config* cfg, const vox_chunk_coord* coords,
+                        const uint8_t* nbr_mask, int32_t n, int64_t index_base, int nthreads,
+                        uint64_t* counts, uint64_t* digests) {
+  if (!valid_size(cfg->chunk_size) || n < 0 || !counts) return -1;
+  gen_digest_job j;
+  memset(&j, 0, sizeof j);
+  j.cfg = cfg;
+  j.coords = coords;
+  j.nbr_mask = nbr_mask;
+  j.n = n;
+  j.index_base = index_base;
+  j.counts = counts;
+  j.digests = digests;
+  if (nthreads < 1) nthreads = 1;
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)nthreads);
+  if (!th) return -1;
+  for (int t = 0; t < nthreads; ++t) pthread_create(&th[t], NULL, gen_digest_worker, &j);
+  for (int t = 0; t < nthreads; ++t) pthread_join(th[t], NULL);
+  free(th);
+  return j.failed ? -1 : 0;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* Camera::update_global_matrix (src/camera.rs:41-51)                                    */
+/* ------------------------------------------------------------------------------------ */
+
+static void or_cross(const float a[3], const float b[3], float out[3]) {
+  out[0] = a[1] * b[2] - a[2] * b[1];
+  out[1] = a[2] * b[0] - a[0] * b[2];
+  out[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+static int or_normalize(float v[3]) {
+  const float len = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+  if (!(len > 0.0f)) return -1;
+  for (int k = 0; k < 3; ++k) v[k] = v[k] / len;
+  return 0;
+}
+
+int or_camera_global_matrix(const float eye[3], const float dir[3], float aspect, float fovy,
+                            float znear, float zfar, float out[16]) {
+  /* look_at_rh(eye, target = eye + dir, up = +y); target - eye is taken as dir itself */
+  const float up[3] = {0.0f, 1.0f, 0.0f};
+  float zaxis[3] = {-dir[0], -dir[1], -dir[2]}, xaxis[3], yaxis[3];
+  if (or_normalize(zaxis)) return -1;
+  or_cross(up, zaxis, xaxis);
+  if (or_normalize(xaxis)) return -1;
+  or_cross(zaxis, xaxis, yaxis);
+  if (or_normalize(yaxis)) return -1;
+  const float* rows[3] = {xaxis, yaxis, zaxis};
+  float V[4][4];
+  for (int r = 0; r < 3; ++r) {
+    for (int c = 0; c < 3; ++c) V[r][c] = rows[r][c];
+    V[r][3] = rows[r][0] * (-eye[0]) + rows[r][1] * (-eye[1]) + rows[r][2] * (-eye[2]);
+  }
+  V[3][0] = V[3][1] = V[3][2] = 0.0f;
+  V[3][3] = 1.0f;
+  /* new_perspective(aspect, fovy, znear, zfar) */
+  float P[4][4];
+  memset(P, 0, sizeof P);
+  P[1][1] = 1.0f / tanf(fovy / 2.0f);
+  P[0][0] = P[1][1] / aspect;
+  P[2][2] = (zfar + znear) / (znear - zfar);
+  P[2][3] = zfar * znear * 2.0f / (znear - zfar);
+  P[3][2] = -1.0f;
+  /* OPENGL_TO_WGPU_MATRIX as camera.rs:18-23 writes it (Matrix4::new takes rows) */
+  static const float G[4][4] = {{1, 0, 0, 0}, {0, 1, 0, 0}, {0, 0, 0.5f, 0}, {0, 0, 0.5f, 1}};
+  float GP[4][4], M[4][4];
+  for (int i = 0; i < 4; ++i)
+    for (int k = 0; k < 4; ++k) {
+      float a = G[i][0] * P[0][k];
+      for (int q = 1; q < 4; ++q) a = a + G[i][q] * P[q][k];
+      GP[i][k] = a;
+    }
+  for (int i = 0; i < 4; ++i)
+    for (int k = 0; k < 4; ++k) {
+      float a = GP[i][0] * V[0][k];
+      for (int q = 1; q < 4; ++q) a = a + GP[i][q] * V[q][k];
+      M[i][k] = a;
+    }
+  for (int c = 0; c < 4; ++c)
+    for (int r = 0; r < 4; ++r) out[c * 4 + r] = M[r][c];
+  return 0;
+}
+
+/* ------------------------------------------------------------------------------------ */
 /* Frustum (src/frustum_culling.rs:16-85)                                                */
 /* ------------------------------------------------------------------------------------ */
 

@@ -103,6 +103,33 @@ int64_t or_gen_mesh_batch(const vox_config* cfg, const vox_chunk_coord* coords,
 int64_t or_baseline_run(const vox_config* cfg, const vox_chunk_coord* coords,
                         const uint8_t* nbr_mask, int32_t n, int64_t index_base, int nthreads);
 
+/* 64-bit digest of a byte run (test bookkeeping only): every 8-byte little-endian word w_k
+ * (the tail zero-padded) is folded in as h = mix(h ^ mix(w_k + k * golden gamma)), with
+ * mix = the splitmix64 finaliser and h starting at the length. */
+uint64_t or_digest(const void* bytes, uint64_t len);
+/* Per-chunk digests of a meshed batch already in memory: chunk i's out0 bytes
+ * [offs[i] * b0, offs[i + 1] * b0) -> digests[2i], its out1 bytes (b1 per face; none when
+ * b1 = 0) -> digests[2i + 1]. nthreads threads. */
+void or_chunk_digests(const void* out0, const void* out1, const uint64_t* offs, int32_t n,
+                      int32_t b0, int32_t b1, int nthreads, uint64_t* digests);
+/* or_gen_mesh_batch chunk by chunk on nthreads threads, keeping only per-chunk results:
+ * counts[i] = chunk i's face count and, when digests is not NULL, the or_chunk_digests
+ * pair of its out0 and out1 bytes (chunk-local indices, so a chunk's bytes do not depend
+ * on the rest of the batch). Returns 0, or -1 on a bad size or an allocation failure. */
+int or_gen_mesh_digests(const vox_config* cfg, const vox_chunk_coord* coords,
+                        const uint8_t* nbr_mask, int32_t n, int64_t index_base, int nthreads,
+                        uint64_t* counts, uint64_t* digests);
+
+/* Camera::update_global_matrix (src/camera.rs:41-51):
+ * OPENGL_TO_WGPU_MATRIX * new_perspective(aspect, fovy, znear, zfar) * look_at_rh(eye,
+ * eye + dir, +y), column-major. look_at_rh: z = normalize(eye - target), x = normalize(up x
+ * z), y = normalize(z x x); view rows x, y, z with translation -(row . eye). Perspective
+ * (OpenGL convention): m11 = 1 / tan(fovy / 2), m00 = m11 / aspect, m22 = (zfar + znear) /
+ * (znear - zfar), m23 = zfar * znear * 2 / (znear - zfar), m32 = -1. Returns 0, or -1 for a
+ * degenerate direction. */
+int or_camera_global_matrix(const float eye[3], const float dir[3], float aspect, float fovy,
+                            float znear, float zfar, float out_colmajor[16]);
+
 /* Frustum (src/frustum_culling.rs:16-85). */
 void or_frustum_planes(const float m_colmajor[16], float planes[24]);
 int or_frustum_contains(const float planes[24], vox_chunk_coord coord, int chunk_extent);

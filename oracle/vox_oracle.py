@@ -59,6 +59,13 @@ def load() -> ctypes.CDLL:
         "or_frustum_planes": (None, [_P, _P]),
         "or_frustum_contains": (ctypes.c_int, [_P, _Coord, ctypes.c_int]),
         "or_raster": (None, [_P, _P, _P, ctypes.c_uint64, ctypes.c_int, ctypes.c_int, _P, _P]),
+        "or_digest": (ctypes.c_uint64, [_P, ctypes.c_uint64]),
+        "or_chunk_digests": (None, [_P, _P, _P, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                    ctypes.c_int, _P]),
+        "or_gen_mesh_digests": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32, ctypes.c_int64,
+                                               ctypes.c_int, _P, _P]),
+        "or_camera_global_matrix": (ctypes.c_int, [_P, _P, ctypes.c_float, ctypes.c_float,
+                                                   ctypes.c_float, ctypes.c_float, _P]),
         "or_noise_error_stats": (ctypes.c_int, [_P, _P, ctypes.c_int32,
                                                 ctypes.POINTER(ctypes.c_double),
                                                 ctypes.POINTER(ctypes.c_int64),
@@ -181,6 +188,55 @@ def baseline_run(cfg, coords, masks, index_base: int, nthreads: int) -> int:
     m = None if masks is None else np.ascontiguousarray(np.asarray(masks, np.uint8))
     return int(load().or_baseline_run(_cfg_addr(cfg), _addr(c), _addr(m), len(c), index_base,
                                       nthreads))
+
+
+def _threads(nthreads):
+    return nthreads or os.cpu_count() or 1
+
+
+def digest(data) -> int:
+    """or_digest of a byte buffer (numpy array or bytes)."""
+    a = np.ascontiguousarray(np.frombuffer(data, np.uint8) if isinstance(data, (bytes, bytearray))
+                             else np.asarray(data).view(np.uint8).reshape(-1))
+    return int(load().or_digest(_addr(a), a.nbytes))
+
+
+def chunk_digests(out0, out1, offsets, b0: int, b1: int, nthreads: int = 0) -> np.ndarray:
+    """Per-chunk (out0, out1) digests of a meshed batch held in host memory: (n, 2) uint64."""
+    offs = np.ascontiguousarray(np.asarray(offsets, np.uint64))
+    n = len(offs) - 1
+    o0 = np.ascontiguousarray(out0).view(np.uint8).reshape(-1)
+    o1 = None if b1 == 0 else np.ascontiguousarray(out1).view(np.uint8).reshape(-1)
+    assert o0.nbytes >= int(offs[-1]) * b0 and (o1 is None or o1.nbytes >= int(offs[-1]) * b1)
+    out = np.zeros((n, 2), np.uint64)
+    load().or_chunk_digests(_addr(o0), _addr(o1), _addr(offs), n, b0, b1, _threads(nthreads),
+                            _addr(out))
+    return out
+
+
+def gen_mesh_digests(cfg, coords, masks=None, index_base: int = 0, nthreads: int = 0,
+                     counts_only: bool = False):
+    """Per-chunk face counts and (out0, out1) digests of or_gen_mesh_batch's output, chunk
+    by chunk on nthreads threads (all host threads by default): (counts[n], digests[n, 2])."""
+    c = coords_array(coords)
+    n = len(c)
+    m = None if masks is None else np.ascontiguousarray(np.asarray(masks, np.uint8))
+    counts = np.zeros(n, np.uint64)
+    dig = None if counts_only else np.zeros((n, 2), np.uint64)
+    st = load().or_gen_mesh_digests(_cfg_addr(cfg), _addr(c), _addr(m), n, index_base,
+                                    _threads(nthreads), _addr(counts), _addr(dig))
+    assert st == 0, st
+    return counts, dig
+
+
+def camera_global_matrix(eye, direction, aspect, fovy, znear, zfar) -> np.ndarray:
+    """Camera::update_global_matrix (src/camera.rs:41-51), column-major float32[16]."""
+    e = np.ascontiguousarray(np.asarray(eye, np.float32).reshape(3))
+    d = np.ascontiguousarray(np.asarray(direction, np.float32).reshape(3))
+    out = np.zeros(16, np.float32)
+    st = load().or_camera_global_matrix(_addr(e), _addr(d), aspect, fovy, znear, zfar, _addr(out))
+    assert st == 0, st
+    return out
 
 
 def frustum_planes(m_colmajor) -> np.ndarray:
