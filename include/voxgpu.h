@@ -6,7 +6,8 @@
  * behind crate-internal Rust methods, and every entry point below names the
  * reference function it replaces (file:line inside that project).
  *
- *   Chunk::new / generate_terrain       src/chunk.rs:21-46        -> vox_generate, vox_occ_to_cubes
+ *   Chunk::new / generate_terrain       src/chunk.rs:21-46        -> vox_generate, vox_generate_slots,
+ *                                                                    vox_occ_to_cubes
  *   Chunk::create_mesh / cull_unseen... src/chunk.rs:48-245       -> vox_mesh, vox_mesh_batch
  *   Quad::new / Quad::to_raw            src/quad.rs:14-54         -> emitted records (vox_instance_raw)
  *   vertex.vert instance expansion      src/shaders/vertex.vert:22-27 -> vox_vertex layout
@@ -162,6 +163,14 @@ int vox_query_sizes(const vox_config* cfg, vox_sizes* out);
 int vox_generate(vox_ctx* ctx, const vox_chunk_coord* d_coords, int32_t n,
                  int64_t chunk_index_base, uint32_t* d_occ);
 
+/* vox_generate into a resident pool (the chunks that World.chunks keeps, src/world.rs:14-22,
+ * for later neighbour rebuilds): chunk i's occupancy goes to slot d_slots[i] of d_occ_pool
+ * (pool_slots slots of occ_words_per_chunk words). A slot outside the pool writes nothing
+ * and makes vox_ctx_sync() return VOX_ERR_INVALID. */
+int vox_generate_slots(vox_ctx* ctx, const vox_chunk_coord* d_coords, int32_t n,
+                       int64_t chunk_index_base, uint32_t* d_occ_pool, int32_t pool_slots,
+                       const int32_t* d_slots);
+
 /* Expands occupancy bitmasks to the reference's Vec<Cube> bytes (src/chunk.rs:35-45):
  * one byte per voxel at x + N*z + N*N*y, GRASS = 0 when solid, AIR = 2 otherwise. */
 int vox_occ_to_cubes(vox_ctx* ctx, const uint32_t* d_occ, int32_t n, uint8_t* d_cubes);
@@ -207,8 +216,10 @@ int vox_gen_mesh_batch(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint
  * every GPU that loads the library until the process exits). At most 16384 chunks per
  * call; larger n returns VOX_ERR_INVALID. Runs on `stream` (a cudaStream_t, NULL = the
  * default stream) and waits for it; returns the device-side status (VOX_ERR_CAPACITY,
- * VOX_ERR_TIMEOUT). The first call on a device looks up the scratch array's address
- * (cudaGetSymbolAddress) and should come before any stream capture. All calls share the
+ * VOX_ERR_TIMEOUT). Every call is synchronous, so it must never be made on a stream that is
+ * being captured (it returns VOX_ERR_INVALID there without queueing work). The first call
+ * on a device looks up the scratch array's address (cudaGetSymbolAddress) and keeps it for
+ * the life of the process: do not use the call across cudaDeviceReset. All calls share the
  * scratch: calls whose work overlaps on the GPU race. */
 int vox_gen_mesh_batch_noalloc(const vox_config* cfg, void* stream,
                                const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
@@ -236,6 +247,10 @@ typedef struct vox_tuning {
                           two buffers per warp (one fills while the other is sent) */
   int32_t ctas_per_sm; /* resident CTAs per SM of the persistent grid; 0 = as many as fit */
   int32_t schedule;    /* VOX_SCHEDULE_LOOKBACK, VOX_SCHEDULE_PHASED or VOX_SCHEDULE_OVERLAP */
+  int32_t slab_chunks; /* output slab: chunks per launch. A larger batch is meshed in
+                          consecutive launches of this many chunks, each writing its slab of
+                          the output right after the previous one's (same bytes and offsets
+                          as one launch); 0 = the whole batch in one launch */
 } vox_tuning;
 
 /* Schedules of the fused batch kernel (all write the same bytes):
@@ -254,8 +269,10 @@ int vox_ctx_set_tuning(vox_ctx* ctx, const vox_tuning* tuning);
 
 /* Autotuner: times every candidate launch shape (schedule x CTA size x staging window x
  * CTAs per SM) on the given batch with vox_gen_mesh_batch (same arguments; iters launches each),
- * keeps the fastest in the context and returns it in *out. The outputs of every
- * candidate are identical; the buffers hold the last run's result. */
+ * then, for the fastest shape, the output slab (the whole batch, or halves, quarters and
+ * eighths of it while a launch keeps at least two waves of the grid); keeps the fastest in
+ * the context and returns it in *out. The outputs of every candidate are identical; the
+ * buffers hold the last run's result. */
 int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
                  int32_t n, int64_t chunk_index_base, void* d_out0, void* d_out1,
                  uint64_t cap_faces, uint64_t* d_face_offsets, int32_t iters, vox_tuning* out);

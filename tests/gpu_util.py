@@ -10,8 +10,12 @@ def torch_cuda():
 
 
 def ctx_for(vox, cfg):
+    """A context on torch's current stream. torch's default stream has the handle 0, which
+    the C ABI reads as "create a stream of your own"; pass the legacy default stream
+    (cudaStreamLegacy, handle 1) instead, so that the context's work and the tests' torch
+    work on the default stream stay in one order."""
     torch = torch_cuda()
-    return vox.Context(cfg, stream=torch.cuda.current_stream().cuda_stream)
+    return vox.Context(cfg, stream=torch.cuda.current_stream().cuda_stream or 1)
 
 
 def to_dev(a, dtype=None):

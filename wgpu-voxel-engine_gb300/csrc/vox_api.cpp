@@ -43,6 +43,7 @@ struct vox_ctx {
   int ctas_per_sm = 0;
   int schedule = VOX_SCHEDULE_LOOKBACK;
   int spin_limit = kSpinLimit;
+  int slab_chunks = 0;  // chunks per launch of a batch (0: the whole batch in one launch)
   int batch_grid[4] = {0, 0, 0, 0};   // persistent grid per gen mode (look-back kernel)
   int phased_grid[4] = {0, 0, 0, 0};  // co-resident grid per gen mode (phased kernel)
   int overlap_grid[4] = {0, 0, 0, 0}; // persistent grid per gen mode (overlap kernel)
@@ -84,6 +85,7 @@ struct vox_graph {
   uint32_t* d_counts = nullptr;           // phased: face totals (n)
   size_t state_bytes = 0;
   unsigned long long wiped_at = 0;        // context launch count when d_state was zeroed
+  int launches = 1;                       // kernel launches per replay (slabs of the batch)
 };
 
 namespace {
@@ -181,10 +183,12 @@ int prepare_kernel(vox_ctx* ctx, const void* fn, int smem) {
 }
 
 // Validates a tuning and computes the persistent grid of every generator mode for it.
-int apply_tuning(vox_ctx* ctx, int topt, int stage_faces, int ctas_per_sm, int schedule) {
+int apply_tuning(vox_ctx* ctx, int topt, int stage_faces, int ctas_per_sm, int schedule,
+                 int slab_chunks) {
   const KernelSet& ks = *ctx->ks;
   const int layout = ctx->cfg.layout;
   if (topt < 0 || topt > 1) return fail(ctx, VOX_ERR_INVALID, "unsupported CTA size");
+  if (slab_chunks < 0) return fail(ctx, VOX_ERR_INVALID, "slab_chunks must be >= 0");
   if (stage_faces != 0 && stage_faces != kStageSingle && stage_faces != kStageDouble)
     return fail(ctx, VOX_ERR_INVALID, "stage_faces must be 0 (direct stores), %d or %d",
                 kStageSingle, kStageDouble);
@@ -221,6 +225,7 @@ int apply_tuning(vox_ctx* ctx, int topt, int stage_faces, int ctas_per_sm, int s
   ctx->stage_faces = stage_faces;
   ctx->ctas_per_sm = ctas_per_sm;
   ctx->schedule = schedule;
+  ctx->slab_chunks = slab_chunks;
   for (int gm = 0; gm < 4; ++gm) {
     ctx->batch_grid[gm] = grid[gm];
     ctx->phased_grid[gm] = pgrid[gm];
@@ -259,9 +264,12 @@ int ensure_state(vox_ctx* ctx, size_t n) {
   return VOX_OK;
 }
 
-// Look-back states are tagged with a 24-bit launch epoch; wipe them before a tag can repeat.
+// Look-back states are tagged with a 24-bit launch epoch. A launch advances it by one, and a
+// launch that timed out by at most two (the host moves a failed launch to a fresh epoch), so
+// a wipe every 2^22 launches comes well before a tag can repeat.
+constexpr unsigned long long kStateWipePeriod = 1ull << 22;
 int before_batch_launch(vox_ctx* ctx) {
-  if (ctx->launches > 0 && (ctx->launches & ((1ull << 23) - 1)) == 0 && ctx->d_state) {
+  if (ctx->launches > 0 && (ctx->launches & (kStateWipePeriod - 1)) == 0 && ctx->d_state) {
     VOX_CUDA(ctx, cudaMemsetAsync(ctx->d_state, 0, ctx->state_cap * sizeof(unsigned long long),
                                   ctx->stream),
              "cudaMemsetAsync(state)");
@@ -350,23 +358,57 @@ int issue_batch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out, cudaStream_t s
   return VOX_OK;
 }
 
+// Chunks per launch of a batch of n chunks under the context's tuning.
+int slab_of(const vox_ctx* ctx, int n) {
+  return ctx->slab_chunks > 0 && ctx->slab_chunks < n ? ctx->slab_chunks : n;
+}
+
+// Cuts the batch `a` into launches of `slab` chunks and calls issue(b) for each, in order.
+// Launch k covers chunks [k * slab, ...): its inputs, offsets and chunk-index base are
+// shifted, and its faces follow the previous launch's (base_ptr = its own face_offsets[0],
+// which the previous launch on the same stream wrote as its total), so the slabs together
+// write exactly what one launch over the batch writes.
+template <typename F>
+int for_each_slab(const MeshArgs& a, int slab, F&& issue) {
+  for (int s = 0; s < a.n; s += slab) {
+    MeshArgs b = a;
+    b.n = std::min(slab, a.n - s);
+    b.index_base = a.index_base + s;
+    if (a.coords) b.coords = a.coords + s;
+    if (a.nbr_mask) b.nbr_mask = a.nbr_mask + s;
+    if (a.slots) b.slots = a.slots + s;
+    if (a.nbr_slots) b.nbr_slots = a.nbr_slots + 6 * (size_t)s;
+    b.face_offsets = a.face_offsets + s;
+    b.base_ptr = s == 0 ? nullptr : a.face_offsets + s;
+    const int st = issue(b);
+    if (st != VOX_OK) return st;
+  }
+  return VOX_OK;
+}
+
 // host_out: the outputs are in host memory; the launch stages every warp's faces in one
 // shared-memory buffer and writes them out with plain full-line stores.
 int batch_launch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out = false) {
   int st;
+  const int slab = slab_of(ctx, a.n);
   if (ctx->schedule != VOX_SCHEDULE_LOOKBACK) {  // the spill slots of phases A and C
-    if ((st = ensure_scratch(ctx, (size_t)a.n)) != VOX_OK) return st;
+    if ((st = ensure_scratch(ctx, (size_t)slab)) != VOX_OK) return st;
     a.scratch = ctx->d_scratch;
     a.counts = ctx->d_counts;
   }
-  if (ctx->schedule == VOX_SCHEDULE_PHASED) {
-    ++ctx->launches;
-  } else {  // look-back state words
-    if ((st = ensure_state(ctx, (size_t)a.n)) != VOX_OK) return st;
-    if ((st = before_batch_launch(ctx)) != VOX_OK) return st;
+  if (ctx->schedule != VOX_SCHEDULE_PHASED) {  // look-back state words
+    if ((st = ensure_state(ctx, (size_t)slab)) != VOX_OK) return st;
     a.state = ctx->d_state;
   }
-  return issue_batch(ctx, a, gm, host_out, ctx->stream);
+  return for_each_slab(a, slab, [&](MeshArgs& b) {
+    if (ctx->schedule == VOX_SCHEDULE_PHASED) {
+      ++ctx->launches;
+    } else {
+      const int s2 = before_batch_launch(ctx);
+      if (s2 != VOX_OK) return s2;
+    }
+    return issue_batch(ctx, b, gm, host_out, ctx->stream);
+  });
 }
 
 }  // namespace
@@ -476,8 +518,8 @@ int vox_ctx_create(const vox_config* cfg, void* stream, vox_ctx** out) {
   const int gsmem = ctx->ks->smem_total(VOX_LAYOUT_VERTEX, ctx->ks->gen_threads, 0);
   for (int gm = 1; gm < 4; ++gm)
     if ((st = prepare_kernel(ctx, ctx->ks->generate[gm], gsmem)) != VOX_OK) return cleanup(st);
-  if (apply_tuning(ctx, default_topt(cfg->chunk_size), kStageSingle, 0, kDefaultSchedule) != VOX_OK &&
-      (st = apply_tuning(ctx, 0, 0, 0, kDefaultSchedule)) != VOX_OK)  // no room to stage
+  if (apply_tuning(ctx, default_topt(cfg->chunk_size), kStageSingle, 0, kDefaultSchedule, 0) != VOX_OK &&
+      (st = apply_tuning(ctx, 0, 0, 0, kDefaultSchedule, 0)) != VOX_OK)  // no room to stage
     return cleanup(st);
   ctx->last_error.clear();
   if ((st = ensure_state(ctx, 1024)) != VOX_OK) return cleanup(st);
@@ -564,6 +606,27 @@ int vox_generate(vox_ctx* ctx, const vox_chunk_coord* d_coords, int32_t n,
   a.index_base = chunk_index_base;
   a.coords = d_coords;
   uint32_t* occ = d_occ;
+  void* params[] = {&a, &occ};
+  return launch(ctx, ctx->ks->generate[ctx->gm], n, ctx->ks->gen_threads,
+                ctx->ks->smem_total(VOX_LAYOUT_VERTEX, ctx->ks->gen_threads, 0), params);
+}
+
+int vox_generate_slots(vox_ctx* ctx, const vox_chunk_coord* d_coords, int32_t n,
+                       int64_t chunk_index_base, uint32_t* d_occ_pool, int32_t pool_slots,
+                       const int32_t* d_slots) {
+  vox::TraceRange trace_("vox_generate_slots");
+  if (!ctx) return VOX_ERR_INVALID;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (n < 0 || (n > 0 && (!d_coords || !d_occ_pool || !d_slots)) || pool_slots < 1)
+    return fail(ctx, VOX_ERR_INVALID, "bad arguments");
+  if (n == 0) return VOX_OK;
+  MeshArgs a = base_args(ctx);
+  a.n = n;
+  a.index_base = chunk_index_base;
+  a.coords = d_coords;
+  a.slots = d_slots;
+  a.pool_slots = pool_slots;
+  uint32_t* occ = d_occ_pool;
   void* params[] = {&a, &occ};
   return launch(ctx, ctx->ks->generate[ctx->gm], n, ctx->ks->gen_threads,
                 ctx->ks->smem_total(VOX_LAYOUT_VERTEX, ctx->ks->gen_threads, 0), params);
@@ -884,6 +947,7 @@ int vox_ctx_get_tuning(vox_ctx* ctx, vox_tuning* out) {
   out->stage_faces = ctx->stage_faces;
   out->ctas_per_sm = ctx->ctas_per_sm;
   out->schedule = ctx->schedule;
+  out->slab_chunks = ctx->slab_chunks;
   return VOX_OK;
 }
 
@@ -895,7 +959,7 @@ int vox_ctx_set_tuning(vox_ctx* ctx, const vox_tuning* t) {
     if (ctx->ks->threads[k] == t->threads) topt = k;
   if (topt < 0) return fail(ctx, VOX_ERR_INVALID, "threads must be %d or %d", ctx->ks->threads[0],
                             ctx->ks->threads[1]);
-  return apply_tuning(ctx, topt, t->stage_faces, t->ctas_per_sm, t->schedule);
+  return apply_tuning(ctx, topt, t->stage_faces, t->ctas_per_sm, t->schedule, t->slab_chunks);
 }
 
 int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
@@ -914,9 +978,9 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
   VOX_CUDA(ctx, cudaEventCreate(&e0), "cudaEventCreate");
   VOX_CUDA(ctx, cudaEventCreate(&e1), "cudaEventCreate");
   const int keep_t = ctx->topt, keep_s = ctx->stage_faces, keep_c = ctx->ctas_per_sm,
-            keep_p = ctx->schedule;
+            keep_p = ctx->schedule, keep_l = ctx->slab_chunks;
   float best_ms = 1e30f;
-  int best_t = keep_t, best_s = keep_s, best_c = keep_c, best_p = keep_p;
+  int best_t = keep_t, best_s = keep_s, best_c = keep_c, best_p = keep_p, best_l = 0;
   auto run = [&]() {
     MeshArgs a = base_args(ctx);
     a.n = n;
@@ -929,7 +993,7 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
     a.face_offsets = reinterpret_cast<unsigned long long*>(d_face_offsets);
     return batch_launch(ctx, a, ctx->gm);
   };
-  auto time_candidate = [&](int p, int t, int s, int c) -> bool {  // false: stop (error)
+  auto time_candidate = [&](int p, int t, int s, int c, int l) -> bool {  // false: stop (error)
     if ((st = run()) != VOX_OK) return false;
     cudaEventRecord(e0, ctx->stream);
     for (int k = 0; k < iters && st == VOX_OK; ++k) st = run();
@@ -947,37 +1011,54 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
       best_s = s;
       best_c = c;
       best_p = p;
+      best_l = l;
     }
     return true;
   };
+  // 1. the launch shape, every chunk of the batch in one launch
   bool go = true;
   for (int p = 0; p < 3 && go; ++p)
     for (int t = 0; t < 2 && go; ++t)
       for (int s : stages) {
         int full_grid = 0;
         for (int c : ctas) {
-          if (apply_tuning(ctx, t, s, c, p) != VOX_OK) continue;
+          if (apply_tuning(ctx, t, s, c, p, 0) != VOX_OK) continue;
           const int g = p == VOX_SCHEDULE_PHASED    ? ctx->phased_grid[ctx->gm]
                         : p == VOX_SCHEDULE_OVERLAP ? ctx->overlap_grid[ctx->gm]
                                                     : ctx->batch_grid[ctx->gm];
           if (c == 0) full_grid = g;
           else if (g >= full_grid) continue;  // same grid as c = 0
-          if (!(go = time_candidate(p, t, s, c))) break;
+          if (!(go = time_candidate(p, t, s, c, 0))) break;
         }
         if (!go) break;
       }
+  // 2. the output slab (chunks per launch) for the best shape: halves, quarters and eighths
+  // of the batch, while a launch still holds at least two waves of the persistent grid
+  // (a smaller slab keeps a launch's spilled chunk state and its output run L2-sized)
+  if (go && apply_tuning(ctx, best_t, best_s, best_c, best_p, 0) == VOX_OK) {
+    const int g = best_p == VOX_SCHEDULE_PHASED    ? ctx->phased_grid[ctx->gm]
+                  : best_p == VOX_SCHEDULE_OVERLAP ? ctx->overlap_grid[ctx->gm]
+                                                   : ctx->batch_grid[ctx->gm];
+    for (int div = 2; div <= 8 && go; div *= 2) {
+      const int l = (n + div - 1) / div;
+      if (l < 2 * g) break;
+      if (apply_tuning(ctx, best_t, best_s, best_c, best_p, l) != VOX_OK) continue;
+      go = time_candidate(best_p, best_t, best_s, best_c, l);
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   ctx->last_error.clear();
-  const int st2 = apply_tuning(ctx, best_t, best_s, best_c, best_p);
+  const int st2 = apply_tuning(ctx, best_t, best_s, best_c, best_p, best_l);
   if (st == VOX_OK) st = st2;
   if (st == VOX_OK) st = sync_locked(ctx);
-  if (st != VOX_OK) apply_tuning(ctx, keep_t, keep_s, keep_c, keep_p);
+  if (st != VOX_OK) apply_tuning(ctx, keep_t, keep_s, keep_c, keep_p, keep_l);
   if (out) {
     out->threads = ctx->ks->threads[ctx->topt];
     out->stage_faces = ctx->stage_faces;
     out->ctas_per_sm = ctx->ctas_per_sm;
     out->schedule = ctx->schedule;
+    out->slab_chunks = ctx->slab_chunks;
   }
   return st;
 }
@@ -1032,15 +1113,17 @@ int vox_graph_capture(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8
   a.out1 = d_out1;
   a.cap = cap_faces;
   a.face_offsets = reinterpret_cast<unsigned long long*>(d_face_offsets);
+  const int slab = slab_of(ctx, n);
+  g->launches = (n + slab - 1) / slab;
   if (g->schedule != VOX_SCHEDULE_LOOKBACK) {
-    if ((e = cudaMalloc(&g->d_scratch, (size_t)n * (size_t)ctx->ks->spill_bytes)) != cudaSuccess ||
-        (e = cudaMalloc(&g->d_counts, (size_t)n * sizeof(uint32_t))) != cudaSuccess)
+    if ((e = cudaMalloc(&g->d_scratch, (size_t)slab * (size_t)ctx->ks->spill_bytes)) != cudaSuccess ||
+        (e = cudaMalloc(&g->d_counts, (size_t)slab * sizeof(uint32_t))) != cudaSuccess)
       return bail(cuda_fail(ctx, e, "cudaMalloc(graph scratch)"));
     a.scratch = g->d_scratch;
     a.counts = g->d_counts;
   }
   if (g->schedule != VOX_SCHEDULE_PHASED) {
-    g->state_bytes = (size_t)n * sizeof(unsigned long long);
+    g->state_bytes = (size_t)slab * sizeof(unsigned long long);
     if ((e = cudaMalloc(&g->d_state, g->state_bytes)) != cudaSuccess ||
         (e = cudaMemsetAsync(g->d_state, 0, g->state_bytes, ctx->stream)) != cudaSuccess)
       return bail(cuda_fail(ctx, e, "cudaMalloc(graph state)"));
@@ -1056,7 +1139,7 @@ int vox_graph_capture(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8
     cudaStreamDestroy(cs);
     return bail(cuda_fail(ctx, e, "cudaStreamBeginCapture"));
   }
-  st = issue_batch(ctx, a, ctx->gm, false, cs);
+  st = for_each_slab(a, slab, [&](MeshArgs& b) { return issue_batch(ctx, b, ctx->gm, false, cs); });
   cudaGraph_t graph = nullptr;
   e = cudaStreamEndCapture(cs, &graph);
   cudaStreamDestroy(cs);
@@ -1076,9 +1159,9 @@ int vox_graph_launch(vox_graph* g) {
   if (!g || !g->ctx) return VOX_ERR_INVALID;
   vox_ctx* ctx = g->ctx;
   std::lock_guard<std::mutex> lk(ctx->mu);
-  ++ctx->launches;
+  ctx->launches += (unsigned long long)g->launches;
   // look-back states carry a 24-bit launch epoch: zero them before a tag can repeat
-  if (g->d_state && ctx->launches - g->wiped_at >= (1ull << 23)) {
+  if (g->d_state && ctx->launches - g->wiped_at >= kStateWipePeriod) {
     VOX_CUDA(ctx, cudaMemsetAsync(g->d_state, 0, g->state_bytes, ctx->stream), "cudaMemsetAsync(state)");
     g->wiped_at = ctx->launches;
   }

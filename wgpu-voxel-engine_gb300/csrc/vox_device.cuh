@@ -1005,6 +1005,11 @@ static __device__ unsigned long long lookback(unsigned long long* state, BatchCt
   return excl;
 }
 
+// Global face index of the launch's first face (MeshArgs::base_ptr; one thread reads it).
+__device__ __forceinline__ unsigned long long launch_base(const MeshArgs& a) {
+  return a.base_ptr ? *reinterpret_cast<const volatile unsigned long long*>(a.base_ptr) : 0ull;
+}
+
 // Status mirror of a launch whose caller waits for it (outputs in host memory): the last
 // CTA to finish copies the error word, with kMirrorValid set, into a page-locked host word,
 // so that the host reads the status after the stream sync without a device-to-host copy.
@@ -1462,15 +1467,17 @@ k_mesh_batch(const __grid_constant__ MeshArgs a, const __grid_constant__ TablesD
   s.carve(smem_raw);
   load_tables<N, LAYOUT>(s, &tab);  // the tables travel as a kernel parameter
   __shared__ int s_item;
-  __shared__ unsigned long long s_base;
+  __shared__ unsigned long long s_base, s_base0;
   __shared__ unsigned s_epoch;
   if (threadIdx.x == 0) {
     s_epoch = ld_relaxed_u32(&a.ctl->epoch);
+    s_base0 = launch_base(a);
     __threadfence();
     s_item = (int)atomicAdd(&a.ctl->next, 1u);
   }
   __syncthreads();
   const unsigned epoch = s_epoch;
+  const unsigned long long base0 = s_base0;
   int i = s_item;
   while (true) {
     if (i >= a.n) {
@@ -1491,7 +1498,7 @@ k_mesh_batch(const __grid_constant__ MeshArgs a, const __grid_constant__ TablesD
     const uint32_t total = count_and_scan<N, LAYOUT, T>(s);
     if (threadIdx.x < 32) {
       const unsigned long long excl =
-          lookback(a.state, a.ctl, epoch, i, total, a.spin_limit);
+          base0 + lookback(a.state, a.ctl, epoch, i, total, a.spin_limit);
       if (threadIdx.x == 0) {
         s_base = excl;
         a.face_offsets[i] = excl;
@@ -1564,14 +1571,15 @@ static __device__ unsigned grid_barrier_t0(BatchCtl* ctl, unsigned nblocks, int 
   return gen + 1u;
 }
 
-// Deterministic exclusive scan of counts[0, n) into offs[0, n), total at offs[n]
-// (one CTA of T threads, 8 counts per thread per tile). Returns the total.
+// Deterministic exclusive scan of counts[0, n) into offs[0, n) starting at `base`, base +
+// total at offs[n] (one CTA of T threads, 8 counts per thread per tile). Returns base + total.
 template <int T>
 __device__ unsigned long long scan_counts(const uint32_t* counts, int n,
-                                          unsigned long long* offs, unsigned long long* wsum) {
+                                          unsigned long long* offs, unsigned long long* wsum,
+                                          unsigned long long base) {
   constexpr int V = 8;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarps = T >> 5;
-  unsigned long long carry = 0;
+  unsigned long long carry = base;
   for (int base = 0; base < n; base += T * V) {
     uint32_t v[V];
     unsigned long long local = 0;
@@ -1671,8 +1679,11 @@ k_mesh_batch_phased(const __grid_constant__ MeshArgs a, const __grid_constant__ 
   const unsigned gen = s_gen;
   if (gen == 0xFFFFFFFFu) return;
   if (blockIdx.x == 0) {
+    if (t == 0) s_base = launch_base(a);
+    __syncthreads();
     const unsigned long long total = scan_counts<T>(a.counts, a.n, a.face_offsets,
-                                                    reinterpret_cast<unsigned long long*>(s.stage));
+                                                    reinterpret_cast<unsigned long long*>(s.stage),
+                                                    s_base);
     __syncthreads();
     if (t == 0) {
       if (total > a.cap) atomicOr(&a.ctl->err, ERR_CAPACITY);
@@ -1780,17 +1791,19 @@ k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__
   load_tables<N, LAYOUT>(s, &tab);  // the tables travel as a kernel parameter
   __shared__ unsigned s_item;
   __shared__ unsigned s_epoch;
-  __shared__ unsigned long long s_base;
+  __shared__ unsigned long long s_base, s_base0;
   unsigned char* const spill = reinterpret_cast<unsigned char*>(a.scratch);
   uint4* const fixed16 = reinterpret_cast<uint4*>(s.occ);  // s.halo, s.rows follow s.occ
   const int t = threadIdx.x;
   if (t == 0) {
     s_epoch = ld_relaxed_u32(&a.ctl->epoch);
+    s_base0 = launch_base(a);
     __threadfence();
     s_item = atomicAdd(&a.ctl->next, 1u);
   }
   __syncthreads();
   const unsigned epoch = s_epoch;
+  const unsigned long long base0 = s_base0;
   const unsigned tag = epoch & 0xFFFFFFu;
   const unsigned n = (unsigned)a.n;
   const int split = a.split > 0 ? a.split : 1;
@@ -1872,9 +1885,9 @@ k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__
         // has already found) gives the offset at once.
         w = __shfl_sync(0xffffffffu, w, 0);
         const unsigned long long excl =
-            ((w >> 38) & 3ull) == kFlagIncl
-                ? (w & ((1ull << 38) - 1)) - total
-                : lookback(a.state, a.ctl, epoch, c_i, total, a.spin_limit, false);
+            base0 + (((w >> 38) & 3ull) == kFlagIncl
+                         ? (w & ((1ull << 38) - 1)) - total
+                         : lookback(a.state, a.ctl, epoch, c_i, total, a.spin_limit, false));
         if (t == 0) {
           s_base = excl;
           if (seg == 0) {
@@ -1953,20 +1966,30 @@ k_mesh_single(MeshArgs a) {
   if ((threadIdx.x & 31) == 0) bulk_wait_all();
 }
 
-// Chunk::new for n chunks: one CTA per chunk, occupancy rows written to global memory.
+// Chunk::new for n chunks: one CTA per chunk, occupancy rows written to global memory,
+// chunk i at occ_out + i * words, or at slot a.slots[i] of a pool of a.pool_slots slots when
+// a.slots is set (an out-of-range slot writes nothing and latches ERR_BAD_INPUT).
 template <int N, int GM, int T>
 __global__ void __launch_bounds__(T)
 k_generate(MeshArgs a, uint32_t* occ_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ChunkSmem<N, VOX_LAYOUT_VERTEX> s;
   s.carve(smem_raw);
+  const int i = blockIdx.x;
+  long long slot = i;
+  if (a.slots) {
+    slot = a.slots[i];
+    if (slot < 0 || slot >= a.pool_slots) {
+      if (threadIdx.x == 0) atomicOr(&a.ctl->err, ERR_BAD_INPUT);
+      return;  // uniform across the CTA: no barrier has been reached yet
+    }
+  }
   load_tables<N, VOX_LAYOUT_VERTEX>(s, a.tables);
   __syncthreads();
-  const int i = blockIdx.x;
   gen_chunk<N, GM, VOX_LAYOUT_VERTEX, T>(s, a.gen, a.coords[i], a.index_base + i, 0u, false);
   constexpr int words = N * N * Shape<N>::W;
   const uint32_t* src = reinterpret_cast<const uint32_t*>(s.occ);
-  uint32_t* dst = occ_out + (size_t)i * words;
+  uint32_t* dst = occ_out + (size_t)slot * words;
   for (int q = threadIdx.x; q < words; q += blockDim.x) dst[q] = src[q];
 }
 

@@ -79,6 +79,11 @@ struct MeshArgs {
   int lane_flush;                    // staged faces leave shared memory by plain stores
   int lag;                           // overlap kernel: generation items ahead of emission
   unsigned* err_mirror;              // page-locked host word for the launch's status, or null
+  // Global face index of this launch's first face, or null for 0. A batch cut into several
+  // launches (slabs) points every later launch at its own face_offsets[0], which the previous
+  // launch of the same stream wrote as its total; every offset and output index of the
+  // launch is shifted by it.
+  const unsigned long long* base_ptr;
 };
 
 }  // namespace vox

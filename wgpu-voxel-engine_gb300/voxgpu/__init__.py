@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import ctypes
 import os
+import sys
 import weakref
 from dataclasses import dataclass
 
@@ -66,19 +67,22 @@ class Sizes(ctypes.Structure):
 
 class Tuning(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int32), ("stage_faces", ctypes.c_int32),
-                ("ctas_per_sm", ctypes.c_int32), ("schedule", ctypes.c_int32)]
+                ("ctas_per_sm", ctypes.c_int32), ("schedule", ctypes.c_int32),
+                ("slab_chunks", ctypes.c_int32)]
 
     def as_dict(self):
         return {"threads": self.threads, "stage_faces": self.stage_faces,
                 "ctas_per_sm": self.ctas_per_sm,
                 "schedule": {SCHEDULE_PHASED: "phased", SCHEDULE_OVERLAP: "overlap"}.get(
-                    self.schedule, "lookback")}
+                    self.schedule, "lookback"),
+                "slab_chunks": self.slab_chunks}
 
 
 class ServeConfig(ctypes.Structure):
     _fields_ = [("chunk", Config), ("view_radius", ctypes.c_int32), ("y_min", ctypes.c_int32),
                 ("y_max", ctypes.c_int32), ("max_batch", ctypes.c_int32),
-                ("slots", ctypes.c_int32), ("cache_budget_bytes", ctypes.c_uint64)]
+                ("slots", ctypes.c_int32), ("cache_budget_bytes", ctypes.c_uint64),
+                ("neighbour_rebuild", ctypes.c_int32)]
 
 
 class ServeStats(ctypes.Structure):
@@ -88,7 +92,8 @@ class ServeStats(ctypes.Structure):
                 ("cache_bytes", ctypes.c_uint64), ("resident", ctypes.c_uint64),
                 ("pending", ctypes.c_uint64), ("latency_p50_ms", ctypes.c_double),
                 ("latency_p99_ms", ctypes.c_double), ("latency_max_ms", ctypes.c_double),
-                ("busy_s", ctypes.c_double), ("cancelled", ctypes.c_uint64)]
+                ("busy_s", ctypes.c_double), ("cancelled", ctypes.c_uint64),
+                ("rebuilt", ctypes.c_uint64), ("rebuild_launches", ctypes.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -117,6 +122,8 @@ _SIGS = {
     "vox_ctx_stream": (_P, [_P]),
     "vox_ctx_last_error": (ctypes.c_char_p, [_P]),
     "vox_generate": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int64, _P]),
+    "vox_generate_slots": (ctypes.c_int, [_P, _P, ctypes.c_int32, ctypes.c_int64, _P,
+                                          ctypes.c_int32, _P]),
     "vox_occ_to_cubes": (ctypes.c_int, [_P, _P, ctypes.c_int32, _P]),
     "vox_cubes_to_occ": (ctypes.c_int, [_P, _P, ctypes.c_int32, _P]),
     "vox_mesh": (ctypes.c_int, [_P, _P, ctypes.POINTER(_P), ChunkCoord, _P, _P, ctypes.c_uint64,
@@ -154,6 +161,10 @@ _SIGS = {
     "vox_serve_wait": (ctypes.c_int, [_P, ctypes.c_uint64, ctypes.c_double]),
     "vox_serve_cancel": (ctypes.c_int, [_P, ctypes.c_uint64]),
     "vox_serve_get_stats": (ctypes.c_int, [_P, ctypes.POINTER(ServeStats)]),
+    "vox_serve_latency": (ctypes.c_int, [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_uint64)]),
     "vox_serve_lookup": (ctypes.c_int, [_P, ChunkCoord, ctypes.POINTER(_P), ctypes.POINTER(_P),
                                         ctypes.POINTER(ctypes.c_uint64)]),
     "vox_camera_global_matrix": (ctypes.c_int, [_P, _P, ctypes.c_float, ctypes.c_float,
@@ -255,6 +266,9 @@ class Context:
             self._h = None
 
     def __del__(self):
+        # no CUDA calls while the interpreter shuts down: the runtime may be gone already
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -285,6 +299,12 @@ class Context:
     def generate(self, d_coords, n: int, d_occ, chunk_index_base: int = 0):
         self._check(self._lib.vox_generate(self._h, _ptr(d_coords), n, chunk_index_base,
                                            _ptr(d_occ)), "vox_generate")
+
+    def generate_slots(self, d_coords, n: int, d_pool, pool_slots: int, d_slots,
+                       chunk_index_base: int = 0):
+        self._check(self._lib.vox_generate_slots(self._h, _ptr(d_coords), n, chunk_index_base,
+                                                 _ptr(d_pool), pool_slots, _ptr(d_slots)),
+                    "vox_generate_slots")
 
     def occ_to_cubes(self, d_occ, n: int, d_cubes):
         self._check(self._lib.vox_occ_to_cubes(self._h, _ptr(d_occ), n, _ptr(d_cubes)),
@@ -330,8 +350,8 @@ class Context:
         return t
 
     def set_tuning(self, threads: int, stage_faces: int, ctas_per_sm: int = 0,
-                   schedule: int = 0):
-        t = Tuning(threads, stage_faces, ctas_per_sm, schedule)
+                   schedule: int = 0, slab_chunks: int = 0):
+        t = Tuning(threads, stage_faces, ctas_per_sm, schedule, slab_chunks)
         self._check(self._lib.vox_ctx_set_tuning(self._h, ctypes.byref(t)), "vox_ctx_set_tuning")
 
     def autotune(self, d_coords, d_nbr_mask, n: int, d_out0, d_out1, cap_faces: int, d_offsets,
@@ -387,6 +407,9 @@ class Graph:
             self._h = None
 
     def __del__(self):
+        # no CUDA calls while the interpreter shuts down: the runtime may be gone already
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -409,10 +432,10 @@ class Server:
     """The chunk streaming engine (include/voxgpu_serve.h)."""
 
     def __init__(self, chunk_cfg: Config, view_radius=24, y_min=0, y_max=0, max_batch=64,
-                 slots=3, cache_budget_bytes=24 << 30):
+                 slots=3, cache_budget_bytes=24 << 30, neighbour_rebuild=False):
         self._lib = lib()
         self.cfg = ServeConfig(chunk_cfg, view_radius, y_min, y_max, max_batch, slots,
-                               cache_budget_bytes)
+                               cache_budget_bytes, 1 if neighbour_rebuild else 0)
         h = _P()
         st = self._lib.vox_serve_create(ctypes.byref(self.cfg), ctypes.byref(h))
         if st != VOX_OK:
@@ -425,6 +448,9 @@ class Server:
             self._h = None
 
     def __del__(self):
+        # no CUDA calls while the interpreter shuts down: the runtime may be gone already
+        if sys.is_finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -478,6 +504,17 @@ class Server:
         if st != VOX_OK:
             raise VoxError(st, "vox_serve_get_stats")
         return s
+
+    def latency(self, requested_after=-1e300):
+        """(p50 ms, p99 ms, max ms, count) over requests issued at or after the given
+        engine-clock time."""
+        p50, p99, mx, cnt = (ctypes.c_double(), ctypes.c_double(), ctypes.c_double(),
+                             ctypes.c_uint64())
+        st = self._lib.vox_serve_latency(self._h, requested_after, ctypes.byref(p50),
+                                         ctypes.byref(p99), ctypes.byref(mx), ctypes.byref(cnt))
+        if st != VOX_OK:
+            raise VoxError(st, "vox_serve_latency")
+        return p50.value, p99.value, mx.value, cnt.value
 
     def lookup(self, coord):
         """(device ptr out0, device ptr out1, faces) of a resident chunk, or None."""
