@@ -11,10 +11,14 @@
  * into a device mesh cache kept under a byte budget with least-recently-used eviction.
  * It records, per chunk, the time from its request to the moment its mesh is resident.
  *
- * Unlike the reference (one chunk dispatched and one integrated per 7 frames, meshes
- * rebuilt as neighbours arrive), a chunk's halo comes from the generator itself, so its
- * mesh is the final one (all four lateral neighbours present) whatever else is loaded:
- * the same bytes alone, in any batch, and in any order of arrival.
+ * By default, unlike the reference (one chunk dispatched and one integrated per 7 frames,
+ * meshes rebuilt as neighbours arrive), a chunk's halo comes from the generator itself, so
+ * its mesh is the final one (all four lateral neighbours present) whatever else is loaded:
+ * the same bytes alone, in any batch, and in any order of arrival. With
+ * neighbour_rebuild = 1 the engine keeps the reference's semantics instead: occupancy stays
+ * resident, a chunk's halo comes from its resident neighbours, and the neighbours are
+ * remeshed as chunks arrive, so that once the engine is drained every resident chunk's
+ * mesh is the one the reference builds with its resident neighbours.
  */
 #ifndef VOXGPU_SERVE_H
 #define VOXGPU_SERVE_H
@@ -35,6 +39,13 @@ typedef struct vox_serve_config {
   int32_t max_batch;           /* chunks per launch */
   int32_t slots;               /* batches in flight at once (one stream each) */
   uint64_t cache_budget_bytes; /* device bytes for resident meshes (LRU eviction beyond) */
+  int32_t neighbour_rebuild;   /* 0: every halo from the generator (a chunk's first mesh is
+                                  final); 1: the reference's semantics: a chunk is meshed
+                                  against the neighbours resident at launch (absent ones
+                                  emit their border faces) and remeshed from its cached
+                                  occupancy when a neighbour arrives or leaves. Mode 1 also
+                                  holds a device occupancy pool of one slot per chunk that
+                                  the budget can hold at 4 N^2 faces per chunk */
 } vox_serve_config;
 
 typedef struct vox_serve_stats {
@@ -52,6 +63,8 @@ typedef struct vox_serve_stats {
   double latency_max_ms;
   double busy_s;               /* wall time between the first request and the last completion */
   uint64_t cancelled;          /* requests withdrawn by vox_serve_cancel */
+  uint64_t rebuilt;            /* meshes rebuilt from cached occupancy (neighbour_rebuild) */
+  uint64_t rebuild_launches;   /* mesh-only launches of those rebuilds */
 } vox_serve_stats;
 
 typedef struct vox_serve vox_serve;
@@ -98,6 +111,12 @@ int vox_serve_cancel(vox_serve* s, uint64_t id);
 int vox_serve_drain(vox_serve* s);
 
 int vox_serve_get_stats(vox_serve* s, vox_serve_stats* out);
+
+/* Request -> resident latency over the completed requests issued at or after
+ * requested_after_s (engine clock): p50, p99 and max in ms and their count; for example the
+ * steady state after the first view fill. Any output pointer may be NULL. */
+int vox_serve_latency(vox_serve* s, double requested_after_s, double* p50_ms, double* p99_ms,
+                      double* max_ms, uint64_t* count);
 
 /* The resident mesh of chunk `c`: device pointers to its records (out1 NULL for the
  * instanced layout) and its face count. Returns VOX_ERR_INVALID if it is not resident. */

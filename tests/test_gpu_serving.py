@@ -166,3 +166,125 @@ def test_cache_budget_exhaustion_reports_oom_and_recovers(vox):
     st = server.stats()
     assert st.launches == 0 and st.pending == 0 and st.resident == 0 and st.cancelled == 3
     server.close()
+
+
+LATERAL = ((-1, 0), (1, 0), (0, -1), (0, 1))
+
+
+def oracle_mesh_with(oracle, cfg, c, present):
+    """The oracle's mesh of chunk c with the lateral neighbours in `present` loaded and the
+    others absent (their border faces emitted, src/chunk.rs:102-107)."""
+    adj = []
+    for dx, dz in LATERAL:
+        q = (c[0] + dx, c[1], c[2] + dz)
+        adj.append(oracle.generate_cubes(cfg, q, 0) if q in present else None)
+    return oracle.mesh_chunk(cfg, c, oracle.generate_cubes(cfg, c, 0), adj)
+
+
+def check_resident_against_oracle(server, oracle, cfg, coords):
+    """Every resident chunk of `coords` has the mesh the reference builds with its resident
+    lateral neighbours; returns the resident set."""
+    present = {c for c in coords if server.lookup(c) is not None}
+    for c in present:
+        p0, p1, faces = server.lookup(c)
+        w0, w1, cnt = oracle_mesh_with(oracle, cfg, c, present)
+        assert faces == cnt, (c, faces, cnt)
+        assert np.array_equal(fetch(p0, faces * 96), w0), c
+        assert np.array_equal(fetch(p1, faces * 24), w1), c
+    return present
+
+
+def test_neighbour_rebuild_remeshes_when_a_neighbour_arrives(vox, oracle):
+    """neighbour_rebuild = 1 (src/chunk_builder.rs:89-112, 269-300, 310-332): a chunk meshed
+    before its neighbour arrives has its border faces; once the neighbour is resident the
+    chunk is remeshed from its cached occupancy and equals the oracle with the neighbour."""
+    cfg = vox.workload("heightmap").config()
+    server = vox.Server(cfg, view_radius=4, max_batch=8, slots=2, neighbour_rebuild=True)
+    a, b = (3, 0, -2), (4, 0, -2)
+    ida = server.submit([a])[0]
+    assert server.wait(ida, 30.0) == vox.VOX_OK
+    server.drain()
+    p0, p1, faces = server.lookup(a)
+    w0, w1, cnt = oracle_mesh_with(oracle, cfg, a, set())
+    alone = faces
+    assert faces == cnt and np.array_equal(fetch(p0, faces * 96), w0)
+    idb = server.submit([b])[0]
+    assert server.wait(idb, 30.0) == vox.VOX_OK
+    server.drain()
+    check_resident_against_oracle(server, oracle, cfg, [a, b])
+    assert server.lookup(a)[2] < alone  # the shared border is culled now
+    st = server.stats()
+    assert st.rebuilt >= 1 and st.rebuild_launches >= 1 and st.completed == 2
+    server.close()
+
+
+def test_neighbour_rebuild_converges_in_any_arrival_order(vox, oracle):
+    """Chunks of an 8 x 8 area requested in random waves, some batches in flight together,
+    a few requests cancelled: once drained, every resident chunk equals the oracle with its
+    resident neighbours."""
+    cfg = vox.workload("heightmap").config()
+    rng = np.random.default_rng(3)
+    coords = [(x, 0, z) for z in range(-4, 4) for x in range(-4, 4)]
+    order = [coords[i] for i in rng.permutation(len(coords))]
+    server = vox.Server(cfg, view_radius=4, max_batch=5, slots=3, neighbour_rebuild=True)
+    cancelled = set()
+    for k in range(0, len(order), 9):
+        ids = server.submit(order[k:k + 9])
+        if k == 18:
+            server.cancel(ids[0])
+            cancelled.add(order[k])
+    server.drain()
+    present = check_resident_against_oracle(server, oracle, cfg, coords)
+    assert present == set(coords) - cancelled
+    server.close()
+
+
+def test_neighbour_rebuild_after_eviction(vox, oracle):
+    """A cache budget that holds about 20 chunks: evictions free occupancy slots and queue
+    rebuilds of the neighbours that saw the evicted chunk; after draining, the resident
+    chunks still equal the oracle with their resident neighbours."""
+    cfg = vox.workload("heightmap").config()
+    per_chunk = 4 * 16 * 16 * 120
+    server = vox.Server(cfg, view_radius=4, max_batch=4, slots=2, neighbour_rebuild=True,
+                        cache_budget_bytes=20 * per_chunk)
+    coords = [(x, 0, z) for z in range(6) for x in range(6)]
+    for k in range(0, len(coords), 4):
+        server.submit(coords[k:k + 4])
+        server.drain()
+    st = server.stats()
+    assert st.evicted > 0
+    present = check_resident_against_oracle(server, oracle, cfg, coords)
+    assert 0 < len(present) <= 20
+    server.close()
+
+
+def test_neighbour_rebuild_with_the_camera(vox, oracle):
+    """The camera-driven loop in neighbour-rebuild mode: requests, batches and rebuilds
+    interleave over 60 frames; drained, the resident chunks equal the oracle."""
+    cfg = vox.workload("heightmap").config()
+    server = vox.Server(cfg, view_radius=8, max_batch=32, slots=3, neighbour_rebuild=True)
+    run_frames(vox, server, 60)
+    st = server.stats()
+    assert st.completed == st.requested and st.rebuilt > 0
+    eye, _ = vox.serving_camera(60 / 60)
+    centre = vox.lib().vox_world_to_chunk((ctypes.c_float * 3)(*eye), 16)
+    area = [(centre.x + dx, 0, centre.z + dz) for dz in range(-9, 10) for dx in range(-9, 10)]
+    present = check_resident_against_oracle(server, oracle, cfg, area)
+    assert len(present) > 20
+    server.close()
+
+
+def test_latency_since_a_time_and_stats(vox):
+    """vox_serve_latency over the requests issued after a time: the steady-state figures
+    the benchmark reports next to the overall ones."""
+    cfg = vox.workload("heightmap").config()
+    server = vox.Server(cfg, view_radius=8, max_batch=32, slots=3)
+    t0 = vox.Server.now()
+    run_frames(vox, server, 120)
+    p50, p99, mx, cnt = server.latency()
+    st = server.stats()
+    assert cnt == st.completed and p99 == pytest.approx(st.latency_p99_ms)
+    later = server.latency(t0 + 0.5)
+    assert later[3] <= cnt
+    assert server.latency(1e300)[3] == 0
+    server.close()

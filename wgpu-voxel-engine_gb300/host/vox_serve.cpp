@@ -7,6 +7,17 @@
 // with a byte budget and LRU eviction (the reference evicts everything outside a +-5
 // chunk box, chunk_builder.rs:334-352). Only the public C ABI and the CUDA runtime's
 // stream/event/stream-ordered-allocation calls are used here.
+//
+// Two ways to get a chunk's halo:
+//  - generated (the default): every batch regenerates the lateral halo of its chunks from
+//    the generator, so a chunk's first mesh is already its final one;
+//  - neighbour rebuild (vox_serve_config.neighbour_rebuild): the reference's semantics.
+//    Each resident chunk keeps its occupancy in a device pool; a new chunk is meshed
+//    against the neighbours resident when its batch is launched (an absent neighbour's
+//    border faces are emitted, src/chunk.rs:102-107), and when a chunk becomes resident
+//    the resident neighbours whose meshes did not see it are remeshed from the pool
+//    (ChunkGenerator::rebuild_adjacent_chunks and process_rebuild_queue,
+//    src/chunk_builder.rs:89-112, 269-300, 310-332), in mesh-only batches.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -44,6 +55,16 @@ double mono_now() {
   return duration<double>(steady_clock::now().time_since_epoch()).count();
 }
 
+// Neighbour directions in the order of the halo masks: -x, +x, -z, +z, -y, +y.
+constexpr int kDx[6] = {-1, 1, 0, 0, 0, 0};
+constexpr int kDy[6] = {0, 0, 0, 0, -1, 1};
+constexpr int kDz[6] = {0, 0, -1, 1, 0, 0};
+constexpr int kOpposite[6] = {1, 0, 3, 2, 5, 4};
+
+vox_chunk_coord neighbour(const vox_chunk_coord& c, int d) {
+  return {c.x + kDx[d], c.y + kDy[d], c.z + kDz[d]};
+}
+
 // A batch's output block in device memory, shared by the chunks meshed in it.
 struct Block {
   void* out0 = nullptr;
@@ -55,7 +76,7 @@ struct Block {
 
 struct Entry {
   enum State { PENDING, RESIDENT } state = PENDING;
-  bool in_flight = false;  // its batch is on the GPU (a chunk requested again after a
+  bool in_flight = false;  // its load batch is on the GPU (a chunk requested again after a
                            // cancellation waits for its own batch)
   uint64_t id = 0;  // request id (vox_serve_submit / poll / wait)
   double requested_at = 0.0;
@@ -63,7 +84,14 @@ struct Entry {
   std::shared_ptr<Block> block;
   uint64_t offset = 0;
   uint64_t faces = 0;
+  // neighbour-rebuild mode
+  int occ_slot = -1;            // the chunk's occupancy in the pool (resident chunks)
+  uint8_t nbr_used = 0;         // neighbours (halo-mask bits) its current mesh was built with
+  bool rebuild_queued = false;  // waiting in the rebuild queue
+  bool rebuild_in_flight = false;
 };
+
+enum BatchKind { kLoad = 0, kRebuild = 1 };
 
 struct Slot {
   vox_ctx* ctx = nullptr;
@@ -72,11 +100,17 @@ struct Slot {
   cudaEvent_t done = nullptr;   // recorded after its offsets reach the host
   double launched_at = 0.0;     // engine clock when `start` was recorded
   bool busy = false;
+  int kind = kLoad;
+  uint64_t seq = 0;             // launch sequence number
   vox_chunk_coord* d_coords = nullptr;
   uint8_t* d_mask = nullptr;
+  int32_t* d_slots = nullptr;      // neighbour-rebuild mode: occupancy slot per chunk
+  int32_t* d_nbr_slots = nullptr;  // ... and per chunk and direction (-1: absent)
   uint64_t* d_offsets = nullptr;
   uint64_t* h_offsets = nullptr;  // pinned
   std::vector<vox_chunk_coord> chunks;
+  std::vector<int32_t> occ_slots;  // host copies of d_slots
+  std::vector<uint8_t> nbr_used;   // per chunk: the neighbours its mesh is built with
   std::shared_ptr<Block> block;
   uint64_t cap_faces = 0;
 };
@@ -87,9 +121,11 @@ struct vox_serve {
   vox_serve_config cfg{};
   vox_sizes sizes{};
   int n = 0;
+  int dirs = 4;  // halo directions consulted: the lateral four, or all six (VOX_CULL_FULL6)
   uint64_t bytes_per_face = 0;
   uint64_t est_faces_per_chunk = 0;
   std::vector<Slot> slots;
+  uint64_t launch_seq = 0;
   // culling
   vox_ctx* cull_ctx = nullptr;
   cudaStream_t cull_stream = nullptr;
@@ -100,12 +136,21 @@ struct vox_serve {
   size_t cand_cap = 0;
   bool have_center = false;
   vox_chunk_coord center{0, 0, 0};
+  // neighbour-rebuild mode: the occupancy pool and its free slots; a freed slot is reused
+  // only after every batch launched before it was freed has finished (such a batch may
+  // still read it as a neighbour)
+  uint32_t* d_occ_pool = nullptr;
+  int32_t occ_pool_slots = 0;
+  std::vector<int32_t> occ_free;
+  std::vector<std::pair<int32_t, uint64_t>> occ_deferred;  // (slot, launch_seq when freed)
+  std::vector<vox_chunk_coord> rebuild_queue;
   // state
   std::unordered_map<vox_chunk_coord, Entry, CoordHash, CoordEq> entries;
   std::unordered_map<uint64_t, vox_chunk_coord> by_id;  // request id -> chunk
   uint64_t next_id = 1;
   std::vector<vox_chunk_coord> queue;
-  std::vector<double> latencies;
+  bool queue_sorted = true;  // queue in distance order for the current eye
+  std::vector<std::pair<double, double>> latencies;  // (request time, latency in ms)
   vox_serve_stats stats{};
   uint64_t frame = 0;
   double first_request = -1.0, last_completion = -1.0;
@@ -113,6 +158,8 @@ struct vox_serve {
 };
 
 namespace {
+
+bool rebuild_mode(const vox_serve* s) { return s->cfg.neighbour_rebuild != 0; }
 
 void free_block(Block* b) {
   if (b->out0) cudaFreeAsync(b->out0, b->stream);
@@ -128,8 +175,13 @@ float dist2(const vox_serve* s, const vox_chunk_coord& c) {
   return dx * dx + dy * dy + dz * dz;
 }
 
-// Drops one resident chunk's reference to its block (freeing the block at zero).
-void release(vox_serve* s, Entry& e) {
+Entry* resident_entry(vox_serve* s, const vox_chunk_coord& c) {
+  auto it = s->entries.find(c);
+  return it != s->entries.end() && it->second.state == Entry::RESIDENT ? &it->second : nullptr;
+}
+
+// Drops one chunk's reference to its mesh block (freeing the block at zero).
+void release_mesh(vox_serve* s, Entry& e) {
   if (e.block) {
     if (--e.block->refs == 0) {
       s->stats.cache_bytes -= e.block->bytes;
@@ -138,38 +190,116 @@ void release(vox_serve* s, Entry& e) {
     e.block.reset();
   }
   s->stats.faces_resident -= e.faces;
+  e.faces = 0;
 }
 
-// Evicts least-recently-seen resident chunks until `need` more bytes fit in the budget:
-// first those not seen this frame, then (when the visible set alone exceeds the budget)
-// visible ones. Returns false if the budget cannot hold `need` at all.
-bool make_room(vox_serve* s, uint64_t need) {
-  if (need > s->cfg.cache_budget_bytes) return false;
-  while (s->stats.cache_bytes + need > s->cfg.cache_budget_bytes) {
-    auto victim = s->entries.end();
-    for (int pass = 0; pass < 2 && victim == s->entries.end(); ++pass) {
-      for (auto it = s->entries.begin(); it != s->entries.end(); ++it) {
-        if (it->second.state != Entry::RESIDENT) continue;
-        if (pass == 0 && it->second.last_seen >= s->frame) continue;
-        if (victim == s->entries.end() || it->second.last_seen < victim->second.last_seen)
-          victim = it;
-      }
+void free_occ_slot(vox_serve* s, int32_t slot) {
+  if (slot >= 0) s->occ_deferred.emplace_back(slot, s->launch_seq);
+}
+
+// Moves deferred occupancy slots whose readers have all finished to the free list.
+void recycle_occ_slots(vox_serve* s) {
+  uint64_t oldest = UINT64_MAX;  // sequence number of the oldest batch still on the GPU
+  for (const Slot& sl : s->slots)
+    if (sl.busy) oldest = std::min(oldest, sl.seq);
+  size_t keep = 0;
+  for (const auto& d : s->occ_deferred) {
+    if (d.second < oldest) s->occ_free.push_back(d.first);
+    else s->occ_deferred[keep++] = d;
+  }
+  s->occ_deferred.resize(keep);
+}
+
+void queue_rebuild(vox_serve* s, const vox_chunk_coord& c, Entry& e) {
+  if (e.rebuild_queued || e.rebuild_in_flight) return;  // an in-flight rebuild re-checks
+  e.rebuild_queued = true;
+  s->rebuild_queue.push_back(c);
+}
+
+// The halo-mask bits of c's neighbours that are resident now.
+uint8_t resident_neighbours(vox_serve* s, const vox_chunk_coord& c) {
+  uint8_t m = 0;
+  for (int d = 0; d < s->dirs; ++d)
+    if (resident_entry(s, neighbour(c, d))) m |= (uint8_t)(1u << d);
+  return m;
+}
+
+// Evicts one resident chunk: its mesh, its occupancy slot, and (rebuild mode) a rebuild of
+// every resident neighbour whose mesh was built against it.
+void evict(vox_serve* s, std::unordered_map<vox_chunk_coord, Entry, CoordHash, CoordEq>::iterator it) {
+  const vox_chunk_coord c = it->first;
+  Entry& e = it->second;
+  release_mesh(s, e);
+  free_occ_slot(s, e.occ_slot);
+  s->by_id.erase(e.id);
+  s->entries.erase(it);
+  ++s->stats.evicted;
+  --s->stats.resident;
+  if (!rebuild_mode(s)) return;
+  for (int d = 0; d < s->dirs; ++d) {
+    const vox_chunk_coord q = neighbour(c, d);
+    Entry* y = resident_entry(s, q);
+    if (y && ((y->nbr_used >> kOpposite[d]) & 1u)) queue_rebuild(s, q, *y);
+  }
+}
+
+size_t occ_available(vox_serve* s) {
+  recycle_occ_slots(s);
+  return s->occ_free.size();
+}
+
+// Evicts least-recently-seen resident chunks until `need` more mesh bytes fit in the budget
+// and (rebuild mode) `need_occ` occupancy slots are free: first chunks not seen this frame,
+// then (when the visible set alone exceeds the budget) visible ones. Returns false if that
+// cannot be reached now.
+bool evict_lru(vox_serve* s) {
+  auto victim = s->entries.end();
+  for (int pass = 0; pass < 2 && victim == s->entries.end(); ++pass) {
+    for (auto it = s->entries.begin(); it != s->entries.end(); ++it) {
+      // chunks whose rebuild is being launched or is on the GPU stay
+      if (it->second.state != Entry::RESIDENT || it->second.rebuild_in_flight) continue;
+      if (pass == 0 && it->second.last_seen >= s->frame) continue;
+      if (victim == s->entries.end() || it->second.last_seen < victim->second.last_seen)
+        victim = it;
     }
-    if (victim == s->entries.end()) return false;
-    release(s, victim->second);
-    s->by_id.erase(victim->second.id);
-    s->entries.erase(victim);
-    ++s->stats.evicted;
-    --s->stats.resident;
+  }
+  if (victim == s->entries.end()) return false;
+  evict(s, victim);
+  return true;
+}
+
+bool make_room(vox_serve* s, uint64_t need, size_t need_occ) {
+  if (need > s->cfg.cache_budget_bytes) return false;
+  if (rebuild_mode(s) && need_occ > (size_t)s->occ_pool_slots) return false;
+  while (s->stats.cache_bytes + need > s->cfg.cache_budget_bytes)
+    if (!evict_lru(s)) return false;
+  if (need_occ > 0) {
+    // slots freed by evictions are reusable once the batches in flight have finished
+    while (occ_available(s) + s->occ_deferred.size() < need_occ)
+      if (!evict_lru(s)) return false;
+    if (occ_available(s) < need_occ) return false;  // retry when those batches finish
   }
   return true;
 }
 
-int launch_batch(vox_serve* s, Slot& sl, std::vector<vox_chunk_coord>&& chunks) {
+// Launches a batch on slot `sl`: a load batch generates and meshes `chunks` (rebuild mode:
+// occupancy into their pool slots `occ`, halo from resident or same-batch neighbours); a
+// rebuild batch remeshes resident chunks from the pool.
+int launch_batch(vox_serve* s, Slot& sl, int kind, std::vector<vox_chunk_coord>&& chunks,
+                 std::vector<int32_t>&& occ) {
   const int m = (int)chunks.size();
   const uint64_t cap = (uint64_t)m * s->est_faces_per_chunk;
   const uint64_t bytes = cap * s->bytes_per_face;
-  if (!make_room(s, bytes)) return VOX_ERR_OOM;
+  const bool rb = rebuild_mode(s);
+  const size_t need_occ = rb && kind == kLoad && occ.empty() ? (size_t)m : 0;
+  if (!make_room(s, bytes, need_occ)) return VOX_ERR_OOM;
+  if (need_occ) {
+    occ.resize(m);
+    for (int i = 0; i < m; ++i) {
+      occ[i] = s->occ_free.back();
+      s->occ_free.pop_back();
+    }
+  }
   auto blk = std::make_shared<Block>();
   blk->stream = sl.stream;
   blk->bytes = bytes;
@@ -178,31 +308,81 @@ int launch_batch(vox_serve* s, Slot& sl, std::vector<vox_chunk_coord>&& chunks) 
       (b1 && cudaMallocAsync(&blk->out1, cap * b1, sl.stream) != cudaSuccess)) {
     cudaGetLastError();
     free_block(blk.get());
+    for (int32_t o : occ)
+      if (need_occ) s->occ_free.push_back(o);  // never written: reusable at once
     return VOX_ERR_OOM;
   }
   s->stats.cache_bytes += bytes;
-  std::vector<uint8_t> masks(m, s->cfg.chunk.cull_mode == VOX_CULL_FULL6 ? 0x3F : 0x0F);
+  sl.seq = ++s->launch_seq;
   sl.launched_at = mono_now();
   cudaEventRecord(sl.start, sl.stream);
   cudaMemcpyAsync(sl.d_coords, chunks.data(), sizeof(vox_chunk_coord) * m, cudaMemcpyHostToDevice,
                   sl.stream);
-  cudaMemcpyAsync(sl.d_mask, masks.data(), (size_t)m, cudaMemcpyHostToDevice, sl.stream);
-  int st = vox_gen_mesh_batch(sl.ctx, sl.d_coords, sl.d_mask, m, 0, blk->out0, blk->out1, cap,
-                              sl.d_offsets);
+  int st;
+  std::vector<uint8_t> used(m, 0);
+  if (!rb) {
+    std::vector<uint8_t> masks(m, s->cfg.chunk.cull_mode == VOX_CULL_FULL6 ? 0x3F : 0x0F);
+    cudaMemcpyAsync(sl.d_mask, masks.data(), (size_t)m, cudaMemcpyHostToDevice, sl.stream);
+    st = vox_gen_mesh_batch(sl.ctx, sl.d_coords, sl.d_mask, m, 0, blk->out0, blk->out1, cap,
+                            sl.d_offsets);
+  } else {
+    // halo sources: a chunk of this batch, else a resident neighbour's pool slot
+    std::unordered_map<vox_chunk_coord, int32_t, CoordHash, CoordEq> in_batch;
+    if (kind == kLoad)
+      for (int i = 0; i < m; ++i) in_batch.emplace(chunks[i], occ[i]);
+    std::vector<int32_t> nbr((size_t)6 * m, -1);
+    for (int i = 0; i < m; ++i)
+      for (int d = 0; d < s->dirs; ++d) {
+        const vox_chunk_coord q = neighbour(chunks[i], d);
+        int32_t slot = -1;
+        auto b = in_batch.find(q);
+        if (b != in_batch.end()) slot = b->second;
+        else if (const Entry* y = resident_entry(s, q)) slot = y->occ_slot;
+        nbr[(size_t)6 * i + d] = slot;
+        if (slot >= 0) used[i] |= (uint8_t)(1u << d);
+      }
+    cudaMemcpyAsync(sl.d_slots, occ.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, sl.stream);
+    cudaMemcpyAsync(sl.d_nbr_slots, nbr.data(), sizeof(int32_t) * 6 * m, cudaMemcpyHostToDevice,
+                    sl.stream);
+    st = kind == kLoad ? vox_generate_slots(sl.ctx, sl.d_coords, m, 0, s->d_occ_pool,
+                                            s->occ_pool_slots, sl.d_slots)
+                       : VOX_OK;
+    if (st == VOX_OK)
+      st = vox_mesh_batch(sl.ctx, s->d_occ_pool, s->occ_pool_slots, sl.d_slots, sl.d_nbr_slots,
+                          sl.d_coords, m, blk->out0, blk->out1, cap, sl.d_offsets);
+  }
   if (st != VOX_OK) return st;
   cudaMemcpyAsync(sl.h_offsets, sl.d_offsets, sizeof(uint64_t) * (m + 1), cudaMemcpyDeviceToHost,
                   sl.stream);
   cudaEventRecord(sl.done, sl.stream);
   for (const vox_chunk_coord& c : chunks) {
     auto it = s->entries.find(c);
-    if (it != s->entries.end()) it->second.in_flight = true;
+    if (it == s->entries.end()) continue;
+    if (kind == kLoad) it->second.in_flight = true;
+    else it->second.rebuild_in_flight = true;
   }
+  sl.kind = kind;
   sl.chunks = std::move(chunks);
+  sl.occ_slots = std::move(occ);
+  sl.nbr_used = std::move(used);
   sl.block = blk;
   sl.cap_faces = cap;
   sl.busy = true;
-  ++s->stats.launches;
+  if (kind == kLoad) ++s->stats.launches;
+  else ++s->stats.rebuild_launches;
   return VOX_OK;
+}
+
+// After chunk c became resident or was remeshed (rebuild mode): queue a rebuild of every
+// resident neighbour whose mesh did not see c, and of c itself if its resident neighbours
+// changed after its mesh was launched (one arrived, or one it saw was evicted).
+void schedule_rebuilds(vox_serve* s, const vox_chunk_coord& c, Entry& e) {
+  for (int d = 0; d < s->dirs; ++d) {
+    const vox_chunk_coord q = neighbour(c, d);
+    Entry* y = resident_entry(s, q);
+    if (y && !((y->nbr_used >> kOpposite[d]) & 1u)) queue_rebuild(s, q, *y);
+  }
+  if (resident_neighbours(s, c) != e.nbr_used) queue_rebuild(s, c, e);
 }
 
 // Integrates a finished batch; a batch whose output did not fit is relaunched with room
@@ -217,36 +397,83 @@ int integrate(vox_serve* s, Slot& sl, double now) {
     free_block(sl.block.get());
     sl.block.reset();
     s->est_faces_per_chunk = std::max<uint64_t>(s->est_faces_per_chunk, (total + m - 1) / m + 1);
+    const int kind = sl.kind;
+    const std::vector<vox_chunk_coord> keep = sl.chunks;
+    const std::vector<int32_t> keep_occ = sl.occ_slots;
     std::vector<vox_chunk_coord> again = std::move(sl.chunks);
+    std::vector<int32_t> occ = std::move(sl.occ_slots);
     sl.chunks.clear();
-    return launch_batch(s, sl, std::move(again));
+    sl.occ_slots.clear();
+    if (kind == kLoad && s->stats.launches > 0) --s->stats.launches;
+    if (kind == kRebuild && s->stats.rebuild_launches > 0) --s->stats.rebuild_launches;
+    const int st = launch_batch(s, sl, kind, std::move(again), std::move(occ));
+    if (st == VOX_OK) return VOX_OK;
+    // no room to relaunch now: the chunks go back to their queues
+    for (size_t i = 0; i < keep.size(); ++i) {
+      auto it = s->entries.find(keep[i]);
+      if (kind == kLoad) {
+        if (!keep_occ.empty()) free_occ_slot(s, keep_occ[i]);
+        if (it != s->entries.end() && it->second.in_flight) {
+          it->second.in_flight = false;
+          s->queue.push_back(keep[i]);
+          s->queue_sorted = false;
+        }
+      } else if (it != s->entries.end() && it->second.state == Entry::RESIDENT &&
+                 it->second.rebuild_in_flight) {
+        it->second.rebuild_in_flight = false;
+        queue_rebuild(s, keep[i], it->second);
+      }
+    }
+    return st == VOX_ERR_OOM ? VOX_OK : st;
   }
   if (status != VOX_OK) return status;
   sl.block->refs = m;
+  std::vector<vox_chunk_coord> changed;
   for (int i = 0; i < m; ++i) {
-    auto it = s->entries.find(sl.chunks[i]);
-    if (it == s->entries.end() || !it->second.in_flight) {  // cancelled meanwhile
+    const vox_chunk_coord c = sl.chunks[i];
+    auto it = s->entries.find(c);
+    const bool keep = it != s->entries.end() &&
+                      (sl.kind == kLoad ? it->second.in_flight
+                                        : it->second.rebuild_in_flight &&
+                                              it->second.state == Entry::RESIDENT);
+    if (!keep) {  // cancelled or evicted meanwhile
       if (--sl.block->refs == 0) {
         s->stats.cache_bytes -= sl.block->bytes;
         free_block(sl.block.get());
       }
+      if (sl.kind == kLoad && !sl.occ_slots.empty()) free_occ_slot(s, sl.occ_slots[i]);
       continue;
     }
     Entry& e = it->second;
-    e.in_flight = false;
-    e.state = Entry::RESIDENT;
+    if (sl.kind == kLoad) {
+      e.in_flight = false;
+      e.state = Entry::RESIDENT;
+      if (!sl.occ_slots.empty()) e.occ_slot = sl.occ_slots[i];
+      ++s->stats.completed;
+      ++s->stats.resident;
+      --s->stats.pending;
+      s->latencies.emplace_back(e.requested_at, (now - e.requested_at) * 1e3);
+    } else {
+      release_mesh(s, e);
+      e.rebuild_in_flight = false;
+      ++s->stats.rebuilt;
+    }
     e.block = sl.block;
     e.offset = sl.h_offsets[i];
     e.faces = sl.h_offsets[i + 1] - sl.h_offsets[i];
+    e.nbr_used = sl.nbr_used[i];
     s->stats.faces_resident += e.faces;
-    ++s->stats.completed;
-    ++s->stats.resident;
-    --s->stats.pending;
-    s->latencies.push_back((now - e.requested_at) * 1e3);
+    changed.push_back(c);
   }
-  s->last_completion = now;
+  if (rebuild_mode(s))
+    for (const vox_chunk_coord& c : changed) {
+      Entry* e = resident_entry(s, c);
+      if (e) schedule_rebuilds(s, c, *e);
+    }
+  if (sl.kind == kLoad) s->last_completion = now;
   sl.block.reset();
   sl.chunks.clear();
+  sl.occ_slots.clear();
   return VOX_OK;
 }
 
@@ -266,10 +493,17 @@ uint64_t request(vox_serve* s, const vox_chunk_coord& c, double now_s) {
   s->entries.emplace(c, e);
   s->by_id.emplace(e.id, c);
   s->queue.push_back(c);
+  s->queue_sorted = false;
   ++s->stats.requested;
   ++s->stats.pending;
   if (s->first_request < 0.0) s->first_request = now_s;
   return e.id;
+}
+
+bool any_busy(const vox_serve* s) {
+  for (const Slot& sl : s->slots)
+    if (sl.busy) return true;
+  return false;
 }
 
 int poll_and_admit(vox_serve* s, bool wait) {
@@ -288,27 +522,58 @@ int poll_and_admit(vox_serve* s, bool wait) {
     const int st = integrate(s, sl, t_done);
     if (st != VOX_OK) return st;
   }
-  // admit: nearest requests first
+  // admit requests first, nearest first; rebuilds take the slots that are left
+  const uint64_t per_chunk = s->est_faces_per_chunk * s->bytes_per_face;
+  const size_t fit = (size_t)std::max<uint64_t>(1, s->cfg.cache_budget_bytes / per_chunk);
+  const size_t batch = std::min<size_t>((size_t)s->cfg.max_batch, fit);
   if (!s->queue.empty()) {
-    std::sort(s->queue.begin(), s->queue.end(),
-              [s](const vox_chunk_coord& a, const vox_chunk_coord& b) {
-                return dist2(s, a) < dist2(s, b);
-              });
+    if (!s->queue_sorted)
+      std::stable_sort(s->queue.begin(), s->queue.end(),
+                       [s](const vox_chunk_coord& a, const vox_chunk_coord& b) {
+                         return dist2(s, a) < dist2(s, b);
+                       });
+    s->queue_sorted = true;
     size_t head = 0;
-    // a batch reserves est_faces_per_chunk faces per chunk; keep one batch within the budget
-    const uint64_t per_chunk = s->est_faces_per_chunk * s->bytes_per_face;
-    const size_t fit = (size_t)std::max<uint64_t>(1, s->cfg.cache_budget_bytes / per_chunk);
     for (Slot& sl : s->slots) {
       if (sl.busy || head >= s->queue.size()) continue;
-      const size_t take =
-          std::min<size_t>(std::min<size_t>((size_t)s->cfg.max_batch, fit), s->queue.size() - head);
+      const size_t take = std::min<size_t>(batch, s->queue.size() - head);
       std::vector<vox_chunk_coord> chunks(s->queue.begin() + head, s->queue.begin() + head + take);
-      const int st = launch_batch(s, sl, std::move(chunks));
+      const int st = launch_batch(s, sl, kLoad, std::move(chunks), {});
       if (st == VOX_ERR_OOM) break;  // the cache is full of visible chunks: retry later
       if (st != VOX_OK) return st;
       head += take;
     }
     s->queue.erase(s->queue.begin(), s->queue.begin() + head);
+  }
+  if (!s->rebuild_queue.empty() && s->queue.empty()) {
+    for (Slot& sl : s->slots) {
+      if (sl.busy || s->rebuild_queue.empty()) continue;
+      std::vector<vox_chunk_coord> chunks;
+      std::vector<int32_t> occ;
+      size_t used = 0;
+      for (; used < s->rebuild_queue.size() && chunks.size() < batch; ++used) {
+        const vox_chunk_coord c = s->rebuild_queue[used];
+        Entry* e = resident_entry(s, c);
+        if (!e || !e->rebuild_queued) continue;  // evicted since it was queued
+        e->rebuild_queued = false;
+        e->rebuild_in_flight = true;  // not evicted while its batch is being launched
+        chunks.push_back(c);
+        occ.push_back(e->occ_slot);
+      }
+      s->rebuild_queue.erase(s->rebuild_queue.begin(), s->rebuild_queue.begin() + used);
+      if (chunks.empty()) continue;
+      std::vector<vox_chunk_coord> keep = chunks;
+      const int st = launch_batch(s, sl, kRebuild, std::move(chunks), std::move(occ));
+      if (st != VOX_OK)
+        for (const vox_chunk_coord& c : keep)
+          if (Entry* e = resident_entry(s, c)) e->rebuild_in_flight = false;
+      if (st == VOX_ERR_OOM) {  // no room for the new meshes now: back to the queue
+        for (const vox_chunk_coord& c : keep)
+          if (Entry* e = resident_entry(s, c)) queue_rebuild(s, c, *e);
+        break;
+      }
+      if (st != VOX_OK) return st;
+    }
   }
   return VOX_OK;
 }
@@ -356,6 +621,7 @@ int vox_serve_create(const vox_serve_config* cfg, vox_serve** out) {
   int st = vox_query_sizes(&cfg->chunk, &s->sizes);
   if (st != VOX_OK) return st;
   s->n = cfg->chunk.chunk_size;
+  s->dirs = cfg->chunk.cull_mode == VOX_CULL_FULL6 ? 6 : 4;
   s->bytes_per_face = s->sizes.bytes_per_face_out0 + s->sizes.bytes_per_face_out1;
   s->est_faces_per_chunk = (uint64_t)4 * s->n * s->n;
   // keep freed blocks in the stream-ordered pool instead of returning them to the driver
@@ -374,9 +640,23 @@ int vox_serve_create(const vox_serve_config* cfg, vox_serve** out) {
     if ((st = vox_ctx_create(&cfg->chunk, sl.stream, &sl.ctx)) != VOX_OK) return st;
     if (cudaMalloc(&sl.d_coords, sizeof(vox_chunk_coord) * cfg->max_batch) != cudaSuccess ||
         cudaMalloc(&sl.d_mask, (size_t)cfg->max_batch) != cudaSuccess ||
+        cudaMalloc(&sl.d_slots, sizeof(int32_t) * cfg->max_batch) != cudaSuccess ||
+        cudaMalloc(&sl.d_nbr_slots, sizeof(int32_t) * 6 * cfg->max_batch) != cudaSuccess ||
         cudaMalloc(&sl.d_offsets, sizeof(uint64_t) * (cfg->max_batch + 1)) != cudaSuccess ||
         cudaMallocHost(&sl.h_offsets, sizeof(uint64_t) * (cfg->max_batch + 1)) != cudaSuccess)
       return VOX_ERR_OOM;
+  }
+  if (cfg->neighbour_rebuild) {
+    // one occupancy slot per chunk the mesh budget can hold at the estimated faces per
+    // chunk, and at least enough for every batch in flight plus one
+    const uint64_t per_chunk = s->est_faces_per_chunk * s->bytes_per_face;
+    const uint64_t want = std::max<uint64_t>(cfg->cache_budget_bytes / per_chunk,
+                                             (uint64_t)cfg->max_batch * (cfg->slots + 1));
+    s->occ_pool_slots = (int32_t)std::min<uint64_t>(want, 1u << 20);
+    const size_t bytes = (size_t)s->occ_pool_slots * s->sizes.occ_words_per_chunk * 4;
+    if (cudaMalloc(&s->d_occ_pool, bytes) != cudaSuccess) return VOX_ERR_OOM;
+    s->occ_free.reserve(s->occ_pool_slots);
+    for (int32_t k = s->occ_pool_slots - 1; k >= 0; --k) s->occ_free.push_back(k);
   }
   if (cudaStreamCreateWithFlags(&s->cull_stream, cudaStreamNonBlocking) != cudaSuccess)
     return VOX_ERR_CUDA;
@@ -390,13 +670,15 @@ int vox_serve_destroy(vox_serve* s) {
   for (Slot& sl : s->slots) {
     if (sl.stream) cudaStreamSynchronize(sl.stream);
   }
-  for (auto& kv : s->entries) release(s, kv.second);
+  for (auto& kv : s->entries) release_mesh(s, kv.second);
   for (Slot& sl : s->slots) {
     if (sl.block) free_block(sl.block.get());
     if (sl.stream) cudaStreamSynchronize(sl.stream);
     vox_ctx_destroy(sl.ctx);
     cudaFree(sl.d_coords);
     cudaFree(sl.d_mask);
+    cudaFree(sl.d_slots);
+    cudaFree(sl.d_nbr_slots);
     cudaFree(sl.d_offsets);
     if (sl.h_offsets) cudaFreeHost(sl.h_offsets);
     if (sl.done) cudaEventDestroy(sl.done);
@@ -406,6 +688,7 @@ int vox_serve_destroy(vox_serve* s) {
   vox_ctx_destroy(s->cull_ctx);
   cudaFree(s->d_cand);
   cudaFree(s->d_vis);
+  cudaFree(s->d_occ_pool);
   if (s->h_vis) cudaFreeHost(s->h_vis);
   if (s->cull_stream) cudaStreamDestroy(s->cull_stream);
   delete s;
@@ -420,6 +703,7 @@ int vox_serve_frame(vox_serve* s, const float view_proj[16], const float eye[3],
   if (now_s < 0.0) now_s = mono_now();
   ++s->frame;
   ++s->stats.frames;
+  if (std::memcmp(s->eye, eye, sizeof s->eye) != 0) s->queue_sorted = false;
   std::memcpy(s->eye, eye, sizeof s->eye);
   const vox_chunk_coord c = vox_world_to_chunk(eye, s->n);
   int st;
@@ -478,9 +762,7 @@ int vox_serve_wait(vox_serve* s, uint64_t id, double timeout_s) {
     const int32_t r = request_state(s, id);
     if (r == VOX_REQ_RESIDENT) return VOX_OK;
     if (r == VOX_REQ_UNKNOWN) return VOX_ERR_INVALID;
-    bool busy = false;
-    for (Slot& sl : s->slots) busy = busy || sl.busy;
-    if (!busy && !s->queue.empty()) return VOX_ERR_OOM;  // the budget cannot hold its batch
+    if (!any_busy(s) && !s->queue.empty()) return VOX_ERR_OOM;  // the budget cannot hold its batch
     if (mono_now() >= deadline) return VOX_ERR_TIMEOUT;
     std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
@@ -508,34 +790,46 @@ int vox_serve_drain(vox_serve* s) {
   vox::TraceRange trace_("vox_serve_drain");
   if (!s) return VOX_ERR_INVALID;
   for (;;) {
-    bool busy = false;
-    for (Slot& sl : s->slots) busy = busy || sl.busy;
-    if (!busy && s->queue.empty()) return VOX_OK;
+    if (!any_busy(s) && s->queue.empty() && s->rebuild_queue.empty()) return VOX_OK;
     const int st = poll_and_admit(s, true);
     if (st != VOX_OK) return st;
-    bool launched = false;
-    for (Slot& sl : s->slots) launched = launched || sl.busy;
     // nothing in flight and nothing admitted: the budget cannot hold the next batch
-    if (!launched && !s->queue.empty()) return VOX_ERR_OOM;
+    if (!any_busy(s) && (!s->queue.empty() || !s->rebuild_queue.empty())) return VOX_ERR_OOM;
   }
 }
 
 int vox_serve_get_stats(vox_serve* s, vox_serve_stats* out) {
   if (!s || !out) return VOX_ERR_INVALID;
   *out = s->stats;
-  std::vector<double> v = s->latencies;
+  double p50 = 0, p99 = 0, mx = 0;
+  uint64_t cnt = 0;
+  vox_serve_latency(s, -1e300, &p50, &p99, &mx, &cnt);
+  out->latency_p50_ms = p50;
+  out->latency_p99_ms = p99;
+  out->latency_max_ms = mx;
+  out->busy_s = s->first_request >= 0.0 && s->last_completion >= 0.0
+                    ? s->last_completion - s->first_request
+                    : 0.0;
+  return VOX_OK;
+}
+
+int vox_serve_latency(vox_serve* s, double requested_after_s, double* p50_ms, double* p99_ms,
+                      double* max_ms, uint64_t* count) {
+  if (!s) return VOX_ERR_INVALID;
+  std::vector<double> v;
+  v.reserve(s->latencies.size());
+  for (const auto& l : s->latencies)
+    if (l.first >= requested_after_s) v.push_back(l.second);
   auto pct = [&](double q) {
     if (v.empty()) return 0.0;
     size_t k = (size_t)std::min<double>((double)v.size() - 1, std::floor(q * (double)v.size()));
     std::nth_element(v.begin(), v.begin() + (long)k, v.end());
     return v[k];
   };
-  out->latency_p50_ms = pct(0.50);
-  out->latency_p99_ms = pct(0.99);
-  out->latency_max_ms = v.empty() ? 0.0 : *std::max_element(v.begin(), v.end());
-  out->busy_s = s->first_request >= 0.0 && s->last_completion >= 0.0
-                    ? s->last_completion - s->first_request
-                    : 0.0;
+  if (p50_ms) *p50_ms = pct(0.50);
+  if (p99_ms) *p99_ms = pct(0.99);
+  if (max_ms) *max_ms = v.empty() ? 0.0 : *std::max_element(v.begin(), v.end());
+  if (count) *count = (uint64_t)v.size();
   return VOX_OK;
 }
 
