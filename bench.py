@@ -1,13 +1,20 @@
 #!/usr/bin/env python3
 """Benchmark of the chunk generation + meshing path (one JSON line on stdout).
 
-Default workload: 32x32 = 1024 chunks of 16^3 with a 2-D fBm heightmap (4 octaves,
-lacunarity 2, gain 0.5, f = 1/128, seed 7, amplitude 48, base 8), meshed in the
-vertex layout (4 x 24-byte vertices + 6 u32 indices per face). One step = one fused
-generation + meshing launch over the whole batch (vox_gen_mesh_batch). The same batch
-is also run through the plain per-chunk path (one generate + one mesh launch per
-chunk) and end to end through the host-pointer entry point (vox_gen_mesh_host, pinned
-host buffers, copies inside the timed region).
+Headline workload: 32x32 = 1024 chunks of 16^3 with a 2-D fBm heightmap (4 octaves,
+lacunarity 2, gain 0.5, f = 1/128, seed 7, amplitude 48, base 8), meshed in the vertex
+layout (4 x 24-byte vertices + 6 u32 indices per face). One step = one pass of the fused
+generation + meshing path over the whole batch, replayed from a captured CUDA graph with
+the autotuned launch shape and output slab. The same line also carries:
+  - plain_per_chunk: the plain per-chunk GPU path (one generate + one mesh launch per
+    chunk), replayed from a captured graph so that no host work is timed;
+  - e2e: the same batch through vox_gen_mesh_host with page-locked host buffers;
+  - mesh_from_occupancy: the rebuild path (vox_mesh_batch over resident occupancy),
+    byte-compared with the fused output;
+  - stress / density: the 2048 x 64^3 Bernoulli and the 4096 x 32^3 3-D density workloads
+    measured the same way, with their own clocks, rooflines and CPU baselines;
+  - serving: 10,000 real-time frames of the streaming engine (p50/p99 request-to-mesh
+    latency, overall and after the first view fill) and its unpaced capacity.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--workload NAME] [--impl ours|reference]
 
@@ -38,12 +45,36 @@ WORKLOAD_TEXT = {
     "density": "density-fbm3: 16x16x16 chunks of 32^3 (4096), 3-D fBm 3 oct f=1/96 seed 1234, "
                "solid iff fbm-(y-256)/64>0, reference culling, vertex layout",
     "stress": "bernoulli-stress: 2048 isolated chunks of 64^3, Bernoulli(0.5) splitmix64(99^index), "
-              "vertex layout, launched in slabs of --slab chunks",
+              "vertex layout",
 }
+SERVING_TEXT = ("serving: simulated camera 20 u/s + 90 deg/s yaw, 60 frames/s, heightmap-fbm 16^3 "
+                "chunks, view radius 24, 24 GB LRU cache")
 L2_FLUSH_BYTES = 256 << 20
 
+# Per-launch figures of one ncu capture of each kernel on each workload (the command and
+# the other metrics are in the named summary under profiles/). traffic = dram bytes read +
+# written by one launch; for stress the capture ran on 48 chunks and the figure is scaled
+# to the launch's chunk count (DRAM bytes grow with the faces written).
+NCU = {
+    ("k_mesh_batch_overlap", "heightmap"): {
+        "traffic": 7272192, "warp_instructions": 17111898, "chunks": 1024,
+        "summary": "profiles/k_mesh_batch_overlap_heightmap.md"},
+    ("k_mesh_batch_phased", "heightmap"): {
+        "traffic": 6473984, "warp_instructions": 16886488, "chunks": 1024,
+        "summary": "profiles/k_mesh_batch_phased_heightmap.md"},
+    ("k_mesh_batch_overlap", "density"): {
+        "traffic": 683480320, "warp_instructions": 1625252837, "chunks": 4096,
+        "summary": "profiles/k_mesh_batch_overlap_density.md"},
+    ("k_mesh_batch_overlap", "stress"): {
+        "traffic": 47920683349, "chunks": 1024, "scaled_from_chunks": 48,
+        "summary": "profiles/k_mesh_batch_overlap_stress.md"},
+    ("k_mesh_batch_phased", "stress"): {
+        "traffic": 47919420245, "chunks": 1024, "scaled_from_chunks": 48,
+        "summary": "profiles/k_mesh_batch_phased_stress.md"},
+}
 
-def parse_args():
+
+def parse_args(argv=None):
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=400)
@@ -51,25 +82,28 @@ def parse_args():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--workload", choices=list(WORKLOAD_TEXT) + ["serving"], default="heightmap")
     p.add_argument("--layout", choices=["vertex", "instanced"], default="vertex")
-    p.add_argument("--slab", type=int, default=1024,
-                   help="chunks per launch (stress workload; 1024 x 48 MB of output per launch)")
     p.add_argument("--cpu-seconds", type=float, default=8.0,
-                   help="wall time of the CPU-baseline sample")
+                   help="wall time of the CPU-baseline sample of the headline workload")
     p.add_argument("--e2e-steps", type=int, default=50)
     p.add_argument("--plain-steps", type=int, default=3)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-autotune", action="store_true")
     p.add_argument("--no-graph", action="store_true",
-                   help="launch through vox_gen_mesh_batch instead of replaying captured graphs")
+                   help="launch through vox_gen_mesh_batch instead of replaying a captured graph")
     p.add_argument("--tuning", default=None,
-                   help="force a launch shape 'threads,stage_faces,ctas_per_sm[,schedule]' "
+                   help="force a launch shape 'threads,stage_faces,ctas_per_sm[,schedule[,slab]]' "
                         "(schedule 0 look-back, 1 phased, 2 overlap; no autotune)")
-    p.add_argument("--frames", type=int, default=10000, help="serving workload: frames")
-    p.add_argument("--paced", action="store_true", help="serving workload: real-time 60 fps")
-    p.add_argument("--latency-frames", type=int, default=300,
-                   help="paced serving frames measured for the headline latency (0: skip)")
+    p.add_argument("--no-suite", action="store_true",
+                   help="headline workload only (no stress / density / serving sub-runs)")
+    p.add_argument("--suite-steps", type=int, default=0, help="timed steps of the sub-runs (0: --steps)")
+    p.add_argument("--serving-frames", type=int, default=10000,
+                   help="real-time frames of the serving sub-run (0: skip)")
+    p.add_argument("--capacity-chunks", type=int, default=65536,
+                   help="chunks of the unpaced serving capacity run (0: skip)")
+    p.add_argument("--frames", type=int, default=10000, help="--workload serving: frames")
+    p.add_argument("--paced", action="store_true", help="--workload serving: real-time 60 fps")
     p.add_argument("--tune-iters", type=int, default=5)
-    return p.parse_args()
+    return p.parse_args(argv)
 
 
 def dist_info():
@@ -92,6 +126,14 @@ def shard_workload(wl, rank: int, world: int):
     return voxgpu.Workload(wl.name, wl.cfg_kwargs, coords, wl.index_base, wl.isolated)
 
 
+def config_of(name: str, layout: str):
+    """The workload description both arms print (the same dict, so the lines compare)."""
+    import voxgpu
+    wl = voxgpu.workload(name)
+    return {"workload": WORKLOAD_TEXT[name], "chunks": len(wl.coords),
+            "chunk_size": wl.cfg_kwargs["chunk_size"], "layout": layout}
+
+
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons while the GPU works."""
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -112,6 +154,7 @@ class ClockSampler:
             threading.Thread(target=self._read, daemon=True).start()
         except OSError:
             self.proc = None
+        return self
 
     def _read(self):
         for line in self.proc.stdout:
@@ -152,26 +195,8 @@ def load_peak():
         return 6800.0, "fallback"
 
 
-def profiled_value(kernel: str, workload: str, key: str = "traffic_bytes_per_launch"):
-    """A per-launch figure recorded from an ncu capture in profiles/ (or None)."""
-    path = os.path.join(ROOT, "profiles", f"{kernel}_{workload}.md")
-    try:
-        for line in open(path):
-            if line.startswith(key + ":"):
-                return float(line.split(":", 1)[1].strip())
-    except OSError:
-        pass
-    return None
-
-
-def profiled_traffic(kernel: str, workload: str):
-    """DRAM bytes per launch recorded from an ncu capture in profiles/ (or None)."""
-    return profiled_value(kernel, workload)
-
-
 # Warp-instruction issue capacity: 152 SMs x 4 schedulers x 2.07 GHz (nominal).
 ISSUE_PEAK = 152 * 4 * 2.07e9
-
 
 # FP32 operations of one noise sample-octave in the noise formula (the oracle's
 # or_noise2_f32 / or_noise3_f32 plus one fBm step): floors, fractional parts, fades
@@ -181,6 +206,8 @@ NOISE_OPS = {2: 2 + 2 + 14 + 2 + 4 * 3 + 3 * 3 + 2 + 4, 3: 3 + 3 + 21 + 3 + 8 * 
 # FP32 instruction rate with FMA contraction off (one op per instruction): 152 SMs x 128
 # lanes x 2.07 GHz. Nominal: the measured peaks file has no FP32 figure.
 FP32_OPS_NOMINAL = 152 * 128 * 2.07e9
+FP32_PEAK_SOURCE = ("nominal FP32 instruction rate (152 SMs x 128 lanes x 2.07 GHz, FMA contraction "
+                    "off); the measured-peaks file has no FP32 figure")
 
 
 def noise_report(wl, cfg, masks, ms_per_step):
@@ -202,8 +229,7 @@ def noise_report(wl, cfg, masks, ms_per_step):
     achieved = ops / (ms_per_step / 1e3)
     return {"samples_per_chunk": samples, "octaves": g.octaves, "ops_per_sample_octave": NOISE_OPS[dim],
             "achieved_tops": achieved / 1e12, "peak_tops": FP32_OPS_NOMINAL / 1e12,
-            "peak_source": "nominal FP32 instruction rate (FMA contraction off)",
-            "frac": achieved / FP32_OPS_NOMINAL,
+            "peak_source": FP32_PEAK_SOURCE, "frac": achieved / FP32_OPS_NOMINAL,
             "note": "the fused launch also culls and emits; this is the noise share of the step's "
                     "time budget, not the noise kernel alone"}
 
@@ -214,16 +240,19 @@ def cpu_baseline(wl, cfg, masks, seconds: float, threads: int = 0):
     import vox_oracle
     threads = threads or os.cpu_count() or 1
     coords = list(wl.coords)
+    masks = None if wl.isolated else masks
     # calibrate on a small prefix, then size the sample to the time budget
-    k = min(len(coords), 64)
+    k = min(len(coords), max(threads, 16))
     t = time.perf_counter()
-    vox_oracle.baseline_run(cfg, coords[:k], masks[:k], wl.index_base, threads)
+    vox_oracle.baseline_run(cfg, coords[:k], None if masks is None else masks[:k], wl.index_base,
+                            threads)
     per_chunk = max((time.perf_counter() - t) / k, 1e-7)
-    sample = int(min(len(coords), max(8, seconds / per_chunk / 4)))
+    sample = int(min(len(coords), max(threads, seconds / per_chunk / 4)))
     done, t0 = 0, time.perf_counter()
     passes = 0
     while True:
-        vox_oracle.baseline_run(cfg, coords[:sample], masks[:sample], wl.index_base, threads)
+        vox_oracle.baseline_run(cfg, coords[:sample], None if masks is None else masks[:sample],
+                                wl.index_base, threads)
         done += sample
         passes += 1
         if time.perf_counter() - t0 >= seconds:
@@ -243,12 +272,13 @@ def run_reference(args):
     wl = voxgpu.workload(args.workload)
     layout = voxgpu.LAYOUT_INSTANCED if args.layout == "instanced" else voxgpu.LAYOUT_VERTEX
     cfg = wl.config(layout=layout)
-    masks = wl.masks()
+    masks = None if wl.isolated else wl.masks()
     threads = os.cpu_count() or 1
     coords = list(wl.coords)
     k = min(len(coords), 32)
     t = time.perf_counter()
-    vox_oracle.baseline_run(cfg, coords[:k], masks[:k], wl.index_base, threads)
+    vox_oracle.baseline_run(cfg, coords[:k], None if masks is None else masks[:k], wl.index_base,
+                            threads)
     per_chunk = max((time.perf_counter() - t) / k, 1e-7)
     budget = 90.0 / max(1, args.steps + args.warmup)  # the whole run within ~1.5 minutes
     sample = int(min(len(coords), max(1, budget / per_chunk)))
@@ -259,7 +289,8 @@ def run_reference(args):
     def step():
         done, t0 = 0, time.perf_counter()
         while True:
-            vox_oracle.baseline_run(cfg, coords[:sample], masks[:sample], wl.index_base, threads)
+            vox_oracle.baseline_run(cfg, coords[:sample], None if masks is None else masks[:sample],
+                                    wl.index_base, threads)
             done += sample
             if time.perf_counter() - t0 >= window:
                 return done, time.perf_counter() - t0
@@ -275,9 +306,7 @@ def run_reference(args):
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD_TEXT[args.workload], "chunks": len(coords),
-                   "chunk_size": cfg.chunk_size, "layout": args.layout,
-                   "chunks_per_step": sample},
+        "config": config_of(args.workload, args.layout),
         "cpu_baseline": {"value": value, "unit": "chunks/s", "cores": threads, "kind": "port",
                          "sample": f"passes over {sample} of {len(coords)} chunks for about "
                                    f"{window:.1f} s per step; the reference is Rust (no toolchain "
@@ -289,296 +318,215 @@ def run_reference(args):
     return 0
 
 
-def run_ours(args):
-    import numpy as np
-    import torch
-
-    import voxgpu
-
-    rank, world, local = dist_info()
-    torch.cuda.set_device(local)
+def timed_steps(step, steps, stream, flush, torch, world=1):
+    """Exactly `steps` calls of step(), L2 flushed before each (outside the events), CUDA
+    events on the launching stream around each; returns (per-step ms, wall s)."""
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
     if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    wl = shard_workload(voxgpu.workload(args.workload), rank, world)
-    layout = voxgpu.LAYOUT_INSTANCED if args.layout == "instanced" else voxgpu.LAYOUT_VERTEX
-    cfg = wl.config(layout=layout)
-    masks = wl.masks()
-    n_all = len(wl.coords)
-    stream = torch.cuda.Stream()
-    ctx = voxgpu.Context(cfg, stream=stream.cuda_stream)
-    b0, b1 = ctx.sizes.bytes_per_face_out0, ctx.sizes.bytes_per_face_out1
-    slab = args.slab if args.workload == "stress" else n_all
-    slabs = [(s, min(n_all, s + slab)) for s in range(0, n_all, slab)]
-    d_coords = torch.tensor(wl.coords, dtype=torch.int32, device="cuda")
-    d_mask = torch.tensor(masks, dtype=torch.uint8, device="cuda")
-    d_offs = torch.zeros(n_all + len(slabs), dtype=torch.int64, device="cuda")
-
-    # size the output from one sizing pass (the output is deterministic)
-    max_slab_faces = 0
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
     with torch.cuda.stream(stream):
-        probe_cap = 0
-        for si, (a, b) in enumerate(slabs):
-            offs = d_offs[a + si:b + si + 1]
-            ctx.gen_mesh_batch(d_coords[a:b], d_mask[a:b], b - a, None, None, probe_cap, offs,
-                               chunk_index_base=wl.index_base + a)
-            ctx.sync(raise_on_error=False)
-            max_slab_faces = max(max_slab_faces, int(offs[-1].item()))
-    cap = max_slab_faces
-    o0 = torch.empty(cap * b0 + 16, dtype=torch.uint8, device="cuda")
-    o1 = torch.empty(cap * b1 + 16, dtype=torch.uint8, device="cuda") if b1 else None
-    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
-    total_faces = 0
-    # launch shape from the autotuner, timed on the first slab (setup, not timed)
-    tuning = None
-    if args.tuning:
-        ctx.set_tuning(*(int(v) for v in args.tuning.split(",")))
-    elif not args.no_autotune:
-        a, b = slabs[0]
-        with torch.cuda.stream(stream):
-            tuning = ctx.autotune(d_coords[a:b], d_mask[a:b], b - a, o0, o1, cap, d_offs[a:b + 1],
-                                  chunk_index_base=wl.index_base + a, iters=args.tune_iters)
-    tuning = ctx.tuning().as_dict() | {"autotuned": tuning is not None}
-    if rank == 0:
-        print(f"launch shape: {tuning}", file=sys.stderr, flush=True)
-
-    # each slab's launch captured once as a CUDA graph and replayed every step
-    graphs = []
-    if not args.no_graph:
-        with torch.cuda.stream(stream):
-            for si, (a, b) in enumerate(slabs):
-                graphs.append(ctx.capture_graph(d_coords[a:b], d_mask[a:b], b - a, o0, o1, cap,
-                                                d_offs[a + si:b + si + 1],
-                                                chunk_index_base=wl.index_base + a))
-
-    def step():
-        if graphs:
-            for g in graphs:
-                g.launch()
-            return
-        for si, (a, b) in enumerate(slabs):
-            ctx.gen_mesh_batch(d_coords[a:b], d_mask[a:b], b - a, o0, o1, cap,
-                               d_offs[a + si:b + si + 1], chunk_index_base=wl.index_base + a)
-
-    sampler = ClockSampler(local)
-    sampler.start()
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            step()
-        ctx.sync()
-        for si, (a, b) in enumerate(slabs):
-            total_faces += int(d_offs[b + si].item())
-        # timed region: exactly K steps, L2 flushed before each, CUDA events on the
-        # launching stream around each step
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-              for _ in range(args.steps)]
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
-        wall0 = time.perf_counter()
-        for k in range(args.steps):
+        for k in range(steps):
             flush.zero_()
             ev[k][0].record(stream)
             step()
             ev[k][1].record(stream)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - wall0
-        st = ctx.sync(raise_on_error=False)
-        assert st == voxgpu.VOX_OK, f"device status {st}"
-        if world > 1:
-            torch.distributed.barrier()
-    step_ms = [a.elapsed_time(b) for a, b in ev]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if world > 1:
+        torch.distributed.barrier()
+    return [a.elapsed_time(b) for a, b in ev], wall
+
+
+def measure_fused(name, args, torch, stream, flush, world=1, rank=0, local=0, headline=False):
+    """One workload through the fused path: the whole batch resident, autotuned shape and
+    slab, graph replays timed with events. Returns a dict of figures."""
+    import voxgpu
+    from voxgpu.batch import BatchRun
+    wl = shard_workload(voxgpu.workload(name), rank, world)
+    layout = voxgpu.LAYOUT_INSTANCED if args.layout == "instanced" else voxgpu.LAYOUT_VERTEX
+    cfg = wl.config(layout=layout)
+    masks = None if wl.isolated else wl.masks()
+    ctx = voxgpu.Context(cfg, stream=stream.cuda_stream)
+    if args.tuning:
+        v = [int(x) for x in args.tuning.split(",")]
+        ctx.set_tuning(*v)
+    steps = args.steps if headline else (args.suite_steps or args.steps)
+    with torch.cuda.stream(stream):
+        run = BatchRun(ctx, wl.coords, masks, wl.index_base,
+                       autotune=not (args.tuning or args.no_autotune), tune_iters=args.tune_iters,
+                       graph=not args.no_graph)
+        for _ in range(args.warmup):
+            run.launch()
+        ctx.sync()
+    sampler = ClockSampler(local).start()
+    step_ms, wall = timed_steps(run.launch, steps, stream, flush, torch, world)
+    clocks = sampler.stop()
+    st = ctx.sync(raise_on_error=False)
+    assert st == voxgpu.VOX_OK, f"device status {st}"
+    n = len(wl.coords)
+    total = run.total_faces
+    b0, b1 = run.b0, run.b1
     dev_ms = sum(step_ms)
     t = torch.tensor([dev_ms], dtype=torch.float64, device="cuda")
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    max_ms = float(t.item())
-    ms_per_step = max_ms / args.steps
-    chunks_all = n_all * world
-    value = chunks_all / (ms_per_step / 1e3)
-
-    # plain per-chunk path: one generate + one mesh launch per chunk
-    plain = None
-    if rank == 0 and args.plain_steps > 0:
-        plain = plain_per_chunk(ctx, wl, cfg, d_coords, stream, args, b0, b1, torch, np)
-
-    # the rebuild path: meshing from resident occupancy (workloads with neighbours)
-    rebuild = None
-    if rank == 0 and len(slabs) == 1 and not wl.isolated:
-        rebuild = mesh_from_occupancy(ctx, wl, cfg, d_coords, n_all, o0, o1, cap, total_faces,
-                                      stream, flush, args, torch, np)
-    # the generation kernel alone (heightmap and density generators)
-    gen_alone = None
-    if rank == 0 and len(slabs) == 1:
-        gen_alone = noise_kernel(ctx, wl, cfg, d_coords, n_all, stream, flush, args, torch)
-    # end to end through the host-pointer entry point (pinned buffers); the stress output
-    # (49 GB per 1024 chunks) is sampled on its first 64 chunks
-    e2e = None
-    if rank == 0:
-        # (within the first slab, whose offsets start at d_offs[0])
-        n_e2e = min(slabs[0][1], 64) if args.workload == "stress" else n_all
-        faces_e2e = total_faces if n_e2e == n_all and len(slabs) == 1 else int(d_offs[n_e2e].item())
-        e2e = e2e_host(ctx, wl, masks, n_e2e, faces_e2e, b0, b1, args, np)
-        if n_e2e < n_all:
-            e2e["sample"] = f"first {n_e2e} of {n_all} chunks"
-    clocks = sampler.stop()
-
+    ms_per_step = float(t.item()) / steps
     peak, peak_kind = load_peak()
-    alg_bytes = total_faces * (b0 + b1) + n_all * (12 + 1) + (n_all + len(slabs)) * 8
+    launches = run.launches_per_step
+    alg_bytes = total * (b0 + b1) + n * (12 + (0 if masks is None else 1)) + (n + 1) * 8
     kernel_ms = statistics.median(step_ms)
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
     kname = {"phased": "k_mesh_batch_phased", "overlap": "k_mesh_batch_overlap"}.get(
-        tuning.get("schedule"), "k_mesh_batch")
-    traffic = profiled_traffic(kname, args.workload)
-    line = {
-        "metric": METRIC, "value": value, "unit": "chunks/s", "n_gpus": world,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32",
-        "data": "synthetic",
-        "config": {"workload": WORKLOAD_TEXT[args.workload], "chunks": n_all,
-                   "chunk_size": cfg.chunk_size, "layout": args.layout,
-                   "faces_per_step": total_faces, "launches_per_step": len(slabs),
-                   "launch": ("vox_gen_mesh_batch" if args.no_graph
-                              else "CUDA graph replay (one captured graph per slab)"),
-                   "tuning": tuning,
-                   "l2": "flushed before every step (256 MiB write, outside the events)",
-                   "parallelism": f"dp{world} (independent chunk batches)"},
-        "voxels_per_s": value * cfg.chunk_size ** 3,
-        "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak,
-                     "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                     "algorithmic_bytes_per_launch": alg_bytes / len(slabs),
-                     "traffic": traffic},
-        "gpu_launches": args.steps * len(slabs),
-        "wall_s_timed_region": wall,
-        "clocks": clocks,
-    }
-    if plain:
-        line["plain_per_chunk"] = plain
-        line["batched_vs_plain"] = value / world / plain["value"]
-    if e2e:
-        line["e2e"] = e2e
-    if rebuild:
-        line["mesh_from_occupancy"] = rebuild
-    if gen_alone:
-        line["noise_kernel"] = gen_alone
-    if rank == 0 and world == 1 and args.latency_frames > 0 and args.workload == "heightmap":
-        # p50/p99 request-to-mesh latency of the streaming engine at the serving request
-        # rate (real-time 60 frames/s camera), next to the batch throughput above
-        line["latency"] = serving_run(args.latency_frames, paced=True)
-    instr = profiled_value(kname, args.workload, "warp_instructions_per_launch")
-    if instr and len(slabs) == 1:
-        # the same launch against the warp-instruction issue rate: for a launch whose
-        # output stays in L2 this, not HBM, is the budget it spends
-        line["issue_roofline"] = {
+        run.tuning.get("schedule"), "k_mesh_batch")
+    prof = NCU.get((kname, name))
+    roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind,
+            "algorithmic_bytes_per_step": alg_bytes, "launches_per_step": launches,
+            "timing": "median CUDA-event time of one step (all its launches), L2 flushed before "
+                      "each step"}
+    if prof:
+        per_launch_chunks = n / launches
+        roof["traffic"] = prof["traffic"] * per_launch_chunks / prof["chunks"]
+        roof["traffic_source"] = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
+                                  f"({prof['summary']})"
+                                  + (f", captured on {prof['scaled_from_chunks']} chunks and scaled "
+                                     "by the chunk count" if "scaled_from_chunks" in prof else "")
+                                  + ("" if per_launch_chunks == prof["chunks"]
+                                     else f", scaled from {prof['chunks']} to {per_launch_chunks:.0f} "
+                                          "chunks per launch"))
+    else:
+        roof["traffic"] = None
+    res = {"value": n * world / (ms_per_step / 1e3), "unit": "chunks/s", "ms_per_step": ms_per_step,
+           "steps": steps, "chunks": n, "voxels_per_s": n * world / (ms_per_step / 1e3) * cfg.chunk_size ** 3,
+           "faces_per_step": total, "launches_per_step": launches, "tuning": run.tuning,
+           "launch": ("vox_gen_mesh_batch" if args.no_graph
+                      else "CUDA graph replay (one captured graph holding every slab launch)"),
+           "l2": "flushed before every step (256 MiB write, outside the events)",
+           "roofline": roof, "clocks": clocks, "wall_s_timed_region": wall,
+           "gpu_launches": steps * launches}
+    if prof and "warp_instructions" in prof and launches == 1:
+        instr = prof["warp_instructions"] * n / prof["chunks"]
+        res["issue_roofline"] = {
             "warp_instructions_per_launch": instr, "achieved": instr / (kernel_ms / 1e3),
-            "peak": ISSUE_PEAK, "unit": "warp instructions/s", "frac": instr / (kernel_ms / 1e3) / ISSUE_PEAK,
-            "peak_source": "nominal (152 SMs x 4 schedulers x 2.07 GHz); instructions from the ncu "
-                           "capture in profiles/"}
-    noise = noise_report(wl, cfg, masks, ms_per_step)
+            "peak": ISSUE_PEAK, "unit": "warp instructions/s",
+            "frac": instr / (kernel_ms / 1e3) / ISSUE_PEAK,
+            "peak_source": "nominal (152 SMs x 4 schedulers x 2.07 GHz); instructions from "
+                           + prof["summary"]}
+    noise = noise_report(wl, cfg, masks if masks is not None else [0] * n, ms_per_step)
     if noise:
-        line["noise_fp32"] = noise
-    if rank == 0 and world == 1 and not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(wl, cfg, masks, args.cpu_seconds * 0.75)
-        line["cpu_baseline_single_thread"] = cpu_baseline(wl, cfg, masks, args.cpu_seconds * 0.25,
-                                                          threads=1)
-    if rank == 0:
-        print(json.dumps(line), flush=True)
-    ctx.close()
-    if world > 1:
-        torch.distributed.destroy_process_group()
-    return 0
+        res["noise_fp32"] = noise
+    extras = {"wl": wl, "cfg": cfg, "masks": masks, "ctx": ctx, "run": run}
+    return res, extras
 
 
-def plain_per_chunk(ctx, wl, cfg, d_coords, stream, args, b0, b1, torch, np):
-    """Chunk::new then create_mesh per chunk, one launch each (no batching)."""
+def plain_per_chunk(ctx, wl, cfg, masks, stream, args, torch, limit):
+    """Chunk::new then create_mesh per chunk, one launch each (no batching), for the first
+    `limit` chunks of the workload: every generate and mesh launch is captured once into a
+    CUDA graph and the graph is replayed, so the time is the GPU's alone. Chunks whose
+    occupancy those meshes read as a neighbour are generated too."""
     n = len(wl.coords)
+    k = min(n, limit)
     words = ctx.sizes.occ_words_per_chunk
-    occ = torch.empty(n * words, dtype=torch.int32, device="cuda")
     per = ctx.sizes.max_faces_per_chunk
-    k = min(n, 256)  # chunks per timed pass (each chunk writes to its own region)
+    b0, b1 = ctx.sizes.bytes_per_face_out0, ctx.sizes.bytes_per_face_out1
+    occ = torch.empty(n * words, dtype=torch.int32, device="cuda")
     o0 = torch.empty(k * per * b0, dtype=torch.uint8, device="cuda")
     o1 = torch.empty(k * per * b1, dtype=torch.uint8, device="cuda") if b1 else None
     cnt = torch.zeros(k, dtype=torch.int64, device="cuda")
-    masks = wl.masks()
+    d_coords = torch.tensor(list(wl.coords), dtype=torch.int32, device="cuda")
     index = {c: i for i, c in enumerate(wl.coords)}
     offs = [(-1, 0, 0), (1, 0, 0), (0, 0, -1), (0, 0, 1), (0, -1, 0), (0, 1, 0)]
+    occp, cp = occ.data_ptr(), d_coords.data_ptr()
     o0p, o1p = o0.data_ptr(), (o1.data_ptr() if o1 is not None else 0)
-    occp = occ.data_ptr()
-    cp = d_coords.data_ptr()
+    gen, meshes = set(range(k)), []
+    for i in range(k):
+        c = wl.coords[i]
+        nb = []
+        for d, (dx, dy, dz) in enumerate(offs):
+            j = index.get((c[0] + dx, c[1] + dy, c[2] + dz))
+            ok = masks is not None and (masks[i] >> d) & 1 and j is not None
+            if ok:
+                gen.add(j)
+            nb.append(occp + 4 * words * j if ok else None)
+        meshes.append((occp + 4 * words * i, nb, c, o0p + i * per * b0,
+                       (o1p + i * per * b1) if b1 else None, cnt.data_ptr() + 8 * i))
+    gen = sorted(gen)
 
     def one_pass():
-        for i in range(k):
-            # Chunk::new for the chunk and its loaded neighbours' occupancy is produced by
-            # the same per-chunk generate launch (one chunk per launch)
+        for i in gen:
             ctx.generate(cp + 12 * i, 1, occp + 4 * words * i, chunk_index_base=wl.index_base + i)
-        for i in range(k):
-            c = wl.coords[i]
-            nb = []
-            for d, (dx, dy, dz) in enumerate(offs):
-                j = index.get((c[0] + dx, c[1] + dy, c[2] + dz))
-                ok = (masks[i] >> d) & 1 and j is not None and j < k
-                nb.append(occp + 4 * words * j if ok else None)
-            ctx.mesh(occp + 4 * words * i, nb, c, o0p + i * per * b0,
-                     (o1p + i * per * b1) if b1 else None, per, cnt.data_ptr() + 8 * i)
+        for (self_p, nb, c, p0, p1, cntp) in meshes:
+            ctx.mesh(self_p, nb, c, p0, p1, per, cntp)
 
+    torch.cuda.synchronize()
     with torch.cuda.stream(stream):
+        one_pass()  # direct launches once (warms the kernels up)
+    ctx.sync()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(stream):
+        g.capture_begin()
         one_pass()
-        ctx.sync()
+        g.capture_end()
+        g.replay()
         torch.cuda.synchronize()
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
         t0.record(stream)
         for _ in range(args.plain_steps):
-            one_pass()
+            g.replay()
         t1.record(stream)
         torch.cuda.synchronize()
+    assert ctx.sync(raise_on_error=False) == 0
     ms = t0.elapsed_time(t1) / args.plain_steps
+    del g
     return {"value": k / (ms / 1e3), "unit": "chunks/s", "chunks_per_pass": k,
-            "launches_per_chunk": 2, "ms_per_pass": ms}
+            "generate_launches": len(gen), "mesh_launches": k, "ms_per_pass": ms,
+            "api": "vox_generate + vox_mesh per chunk, one launch each, captured once as a CUDA "
+                   "graph and replayed (GPU time only, no host dispatch in the events)"}
 
 
-def noise_kernel(ctx, wl, cfg, d_coords, n, stream, flush, args, torch):
+def noise_kernel(ctx, wl, cfg, stream, flush, args, torch):
     """The generation kernel alone (Chunk::new, src/chunk.rs:21-46): vox_generate writes the
     occupancy of every chunk (no halo) to a device pool; its noise FP32 work is samples x
     octaves x the formula's operation count, against the nominal FP32 instruction rate."""
     g = cfg.gen
     if g.kind not in (0, 1):
         return None
+    n = len(wl.coords)
     N = cfg.chunk_size
     samples, dim = (N * N, 2) if g.kind == 0 else (N ** 3, 3)
+    d_coords = torch.tensor(list(wl.coords), dtype=torch.int32, device="cuda")
     pool = torch.empty(n * ctx.sizes.occ_words_per_chunk, dtype=torch.int32, device="cuda")
-    steps = max(3, args.steps // 4)
+    steps = max(3, (args.suite_steps or args.steps) // 4)
     torch.cuda.synchronize()
     with torch.cuda.stream(stream):
         for _ in range(3):
             ctx.generate(d_coords, n, pool, chunk_index_base=wl.index_base)
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-              for _ in range(steps)]
-        for k in range(steps):
-            flush.zero_()
-            ev[k][0].record(stream)
-            ctx.generate(d_coords, n, pool, chunk_index_base=wl.index_base)
-            ev[k][1].record(stream)
-        torch.cuda.synchronize()
+    step_ms, _ = timed_steps(lambda: ctx.generate(d_coords, n, pool, chunk_index_base=wl.index_base),
+                             steps, stream, flush, torch)
     assert ctx.sync(raise_on_error=False) == 0
-    ms = statistics.median(a.elapsed_time(b) for a, b in ev)
+    ms = statistics.median(step_ms)
     ops = n * samples * g.octaves * NOISE_OPS[dim]
     achieved = ops / (ms / 1e3)
     return {"kernel": "k_generate", "ms": ms, "steps": steps, "chunks": n,
             "samples_per_chunk": samples, "octaves": g.octaves,
             "ops_per_sample_octave": NOISE_OPS[dim], "achieved_tops": achieved / 1e12,
-            "peak_tops": FP32_OPS_NOMINAL / 1e12,
-            "peak_source": "nominal FP32 instruction rate (FMA contraction off)",
+            "peak_tops": FP32_OPS_NOMINAL / 1e12, "peak_source": FP32_PEAK_SOURCE,
             "frac": achieved / FP32_OPS_NOMINAL,
             "occupancy_bytes": n * ctx.sizes.occ_words_per_chunk * 4,
             "api": "vox_generate (occupancy to a device pool, L2 flushed before each step)"}
 
 
-def mesh_from_occupancy(ctx, wl, cfg, d_coords, n, o0, o1, cap, total_faces, stream, flush, args,
-                        torch, np):
+def mesh_from_occupancy(ctx, wl, run, stream, flush, args, torch):
     """The rebuild path (ChunkGenerator::process_rebuild_queue, src/chunk_builder.rs:89-112):
     vox_mesh_batch over occupancy already resident in a device pool (filled once by
-    vox_generate, untimed), with the lateral neighbours' slots as the halo source."""
+    vox_generate, untimed), with the lateral neighbours' slots as the halo source. Its output
+    must equal the fused path's byte for byte."""
+    import numpy as np
+    n = run.n
     words = ctx.sizes.occ_words_per_chunk
     pool = torch.empty(n * words, dtype=torch.int32, device="cuda")
     index = {tuple(c): i for i, c in enumerate(wl.coords)}
@@ -589,32 +537,37 @@ def mesh_from_occupancy(ctx, wl, cfg, d_coords, n, o0, o1, cap, total_faces, str
     d_slots = torch.arange(n, dtype=torch.int32, device="cuda")
     d_nbr = torch.from_numpy(nbr).cuda()
     offs = torch.zeros(n + 1, dtype=torch.int64, device="cuda")
-    steps = max(3, args.steps // 4)
+    total = run.total_faces
+    want0 = run.out0[:total * run.b0].clone()
+    want1 = run.out1[:total * run.b1].clone() if run.b1 else None
+    o0 = torch.empty_like(run.out0)
+    o1 = torch.empty_like(run.out1) if run.out1 is not None else None
+    steps = max(3, (args.suite_steps or args.steps) // 4)
     torch.cuda.synchronize()  # the buffers above were filled on the default stream
     with torch.cuda.stream(stream):
-        ctx.generate(d_coords, n, pool, chunk_index_base=wl.index_base)
+        ctx.generate(run.d_coords, n, pool, chunk_index_base=wl.index_base)
         for _ in range(3):
-            ctx.mesh_batch(pool, n, d_slots, d_nbr, d_coords, n, o0, o1, cap, offs)
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-              for _ in range(steps)]
-        for k in range(steps):
-            flush.zero_()
-            ev[k][0].record(stream)
-            ctx.mesh_batch(pool, n, d_slots, d_nbr, d_coords, n, o0, o1, cap, offs)
-            ev[k][1].record(stream)
-        torch.cuda.synchronize()
+            ctx.mesh_batch(pool, n, d_slots, d_nbr, run.d_coords, n, o0, o1, run.cap, offs)
+    step_ms, _ = timed_steps(
+        lambda: ctx.mesh_batch(pool, n, d_slots, d_nbr, run.d_coords, n, o0, o1, run.cap, offs),
+        steps, stream, flush, torch)
     assert ctx.sync(raise_on_error=False) == 0
-    assert int(offs[-1].item()) == total_faces, "the rebuild path must emit the same faces"
-    ms = statistics.median(a.elapsed_time(b) for a, b in ev)
+    same = (torch.equal(offs, run.offsets) and torch.equal(o0[:total * run.b0], want0)
+            and (want1 is None or torch.equal(o1[:total * run.b1], want1)))
+    assert same, "the rebuild path must write the fused path's bytes"
+    ms = statistics.median(step_ms)
     return {"value": n / (ms / 1e3), "unit": "chunks/s", "ms_per_step": ms, "steps": steps,
+            "bytes_equal_to_fused": True,
             "api": "vox_mesh_batch from device-resident occupancy (L2 flushed before each step)"}
 
 
-def e2e_host(ctx, wl, masks, n, total_faces, b0, b1, args, np):
+def e2e_host(ctx, wl, masks, n, total_faces, b0, b1, args):
     """vox_gen_mesh_host with pinned host buffers: the coordinates and neighbour masks
     come from host memory and every emitted face and offset lands in host memory, all
     inside the timed call (the kernel reads and writes the page-locked buffers in place)."""
     import ctypes
+
+    import numpy as np
 
     import voxgpu
     L = voxgpu.lib()
@@ -625,9 +578,10 @@ def e2e_host(ctx, wl, masks, n, total_faces, b0, b1, args, np):
         return p.value
 
     h_coords = pinned(n * 12)
-    h_mask = pinned(n)
-    ctypes.memmove(h_coords, np.asarray(wl.coords, np.int32).tobytes(), n * 12)
-    ctypes.memmove(h_mask, np.asarray(masks, np.uint8).tobytes(), n)
+    h_mask = pinned(n) if masks is not None else None
+    ctypes.memmove(h_coords, np.asarray(wl.coords[:n], np.int32).tobytes(), n * 12)
+    if masks is not None:
+        ctypes.memmove(h_mask, np.asarray(masks[:n], np.uint8).tobytes(), n)
     h0 = pinned(total_faces * b0)
     h1 = pinned(total_faces * b1) if b1 else None
     h_offs = pinned((n + 1) * 8)
@@ -644,10 +598,11 @@ def e2e_host(ctx, wl, masks, n, total_faces, b0, b1, args, np):
         if p:
             L.vox_host_free(p)
     ms = 1e3 * statistics.median(times)
-    moved = n * 13 + (n + 1) * 8 + total_faces * (b0 + b1)
+    h2d = n * (12 + (1 if masks is not None else 0))
+    d2h = (n + 1) * 8 + total_faces * (b0 + b1)
     return {"value": n / (ms / 1e3), "unit": "chunks/s", "ms_per_step": ms,
-            "host_link_gbs": moved / (ms / 1e3) / 1e9,
-            "h2d_bytes_per_step": n * 13, "d2h_bytes_per_step": (n + 1) * 8 + total_faces * (b0 + b1),
+            "host_link_gbs": (h2d + d2h) / (ms / 1e3) / 1e9,
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
             "api": "vox_gen_mesh_host (pinned host buffers: the kernel reads the inputs and "
                    "writes faces and offsets in host memory over NVLink-C2C; synchronous)"}
 
@@ -664,24 +619,172 @@ def serving_run(frames: int, paced: bool, view_radius: int = 24, slots: int = 4,
                         cache_budget_bytes=24 << 30)
     zfar = (view_radius + 2) * 16.0
     t0 = voxgpu.Server.now()
+    late = 0
     for k in range(frames):
         ts = k / 60.0
         if paced:
             while voxgpu.Server.now() - t0 < ts:
                 time.sleep(0.0005)
+            late = max(late, voxgpu.Server.now() - t0 - ts)
         eye, d = voxgpu.serving_camera(ts)
         srv.frame(voxgpu.camera_matrix(eye, d, zfar=zfar), eye)
     srv.drain()
     wall = voxgpu.Server.now() - t0
     st = srv.stats()
+    steady = srv.latency(t0 + 1.0)
     srv.close()
     return {
         "frames": frames, "paced_60fps": paced, "requested": st.requested,
         "completed": st.completed, "launches": st.launches, "evicted": st.evicted,
+        "chunks_per_launch": st.completed / st.launches if st.launches else None,
         "p50_ms": st.latency_p50_ms, "p99_ms": st.latency_p99_ms, "max_ms": st.latency_max_ms,
-        "chunks_per_s_busy": st.completed / st.busy_s if st.busy_s > 0 else None,
+        "steady_state": {"after_s": 1.0, "requests": steady[3], "p50_ms": steady[0],
+                         "p99_ms": steady[1], "max_ms": steady[2],
+                         "note": "requests issued after the first second (the first frame's "
+                                 "view-disk fill excluded)"},
+        "request_rate_chunks_per_s": st.completed / wall if wall > 0 else None,
         "wall_s": wall, "frame_budget_ms": 1000.0 / 60,
+        "max_frame_start_lag_ms": 1e3 * late if paced else None,
     }
+
+
+def serving_capacity(chunks: int, max_batch: int = 1024, slots: int = 4):
+    """Unpaced capacity of the streaming engine: `chunks` requests of the serving terrain
+    (a square of 16^3 chunks) submitted at once and drained; chunks/s from the first request
+    to the last completion (continuous batching over `slots` streams, `max_batch` chunks per
+    launch)."""
+    import voxgpu
+    wl = voxgpu.workload("heightmap")
+    side = int(round(chunks ** 0.5))
+    coords = [(x, 0, z) for z in range(-side // 2, side - side // 2)
+              for x in range(-side // 2, side - side // 2)]
+    srv = voxgpu.Server(wl.config(), view_radius=24, max_batch=max_batch, slots=slots,
+                        cache_budget_bytes=24 << 30)
+    warm = [(x, 0, 10_000) for x in range(max_batch)]
+    srv.submit(warm)
+    srv.drain()
+    srv.close()
+    srv = voxgpu.Server(wl.config(), view_radius=24, max_batch=max_batch, slots=slots,
+                        cache_budget_bytes=24 << 30)
+    t0 = voxgpu.Server.now()
+    srv.submit(coords, now=t0)
+    srv.drain()
+    wall = voxgpu.Server.now() - t0
+    st = srv.stats()
+    srv.close()
+    return {"chunks": len(coords), "completed": st.completed, "launches": st.launches,
+            "chunks_per_launch": st.completed / st.launches if st.launches else None,
+            "max_batch": max_batch, "slots": slots, "busy_s": st.busy_s, "wall_s": wall,
+            "chunks_per_s": st.completed / st.busy_s if st.busy_s > 0 else None,
+            "p50_ms": st.latency_p50_ms, "p99_ms": st.latency_p99_ms,
+            "api": "vox_serve_submit of every chunk at once, then vox_serve_drain"}
+
+
+def sub_workload(name, args, torch, stream, flush, e2e_chunks=None, cpu_seconds=4.0,
+                 plain_limit=0):
+    """A suite entry: the fused path's figures, its end-to-end call, the plain per-chunk GPU
+    path on a prefix and the CPU port on a sample."""
+    res, ex = measure_fused(name, args, torch, stream, flush)
+    wl, cfg, masks, ctx, run = ex["wl"], ex["cfg"], ex["masks"], ex["ctx"], ex["run"]
+    res["config"] = config_of(name, args.layout)
+    if plain_limit and args.plain_steps > 0:
+        res["plain_per_chunk"] = plain_per_chunk(ctx, wl, cfg, masks, stream, args, torch,
+                                                 plain_limit)
+        res["batched_vs_plain"] = res["value"] / res["plain_per_chunk"]["value"]
+    if name == "density":
+        res["noise_kernel"] = noise_kernel(ctx, wl, cfg, stream, flush, args, torch)
+    n = len(wl.coords)
+    n_e2e = min(n, e2e_chunks or n)
+    faces = run.total_faces if n_e2e == n else int(run.offsets[n_e2e].item())
+    run.close()
+    torch.cuda.empty_cache()
+    res["e2e"] = e2e_host(ctx, wl, masks, n_e2e, faces, run.b0, run.b1, args)
+    if n_e2e < n:
+        res["e2e"]["sample"] = f"first {n_e2e} of {n} chunks"
+    if not args.no_cpu:
+        res["cpu_baseline"] = cpu_baseline(wl, cfg, masks, cpu_seconds)
+    ctx.close()
+    torch.cuda.empty_cache()
+    return res
+
+
+def run_ours(args):
+    import torch
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    stream = torch.cuda.Stream()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    res, ex = measure_fused(args.workload, args, torch, stream, flush, world, rank, local,
+                            headline=True)
+    wl, cfg, masks, ctx, run = ex["wl"], ex["cfg"], ex["masks"], ex["ctx"], ex["run"]
+    if rank == 0:
+        print(f"launch shape: {res['tuning']}", file=sys.stderr, flush=True)
+    line = {
+        "metric": METRIC, "value": res["value"], "unit": "chunks/s", "n_gpus": world,
+        "steps": res["steps"], "warmup": args.warmup, "ms_per_step": res["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32",
+        "data": "synthetic",
+        "config": config_of(args.workload, args.layout),
+        "launch": {k: res[k] for k in ("tuning", "launches_per_step", "faces_per_step", "launch",
+                                       "l2")} | {"parallelism": f"dp{world} (independent chunk "
+                                                                "batches, no exchange)"},
+        "voxels_per_s": res["voxels_per_s"],
+        "roofline": res["roofline"],
+        "gpu_launches": res["gpu_launches"],
+        "wall_s_timed_region": res["wall_s_timed_region"],
+        "clocks": res["clocks"],
+    }
+    for k in ("issue_roofline", "noise_fp32"):
+        if k in res:
+            line[k] = res[k]
+    if rank == 0:
+        n = len(wl.coords)
+        if args.plain_steps > 0:
+            limit = {8: 1024, 16: 1024, 32: 256}.get(cfg.chunk_size, 32)
+            line["plain_per_chunk"] = plain_per_chunk(ctx, wl, cfg, masks, stream, args, torch, limit)
+            line["batched_vs_plain"] = res["value"] / world / line["plain_per_chunk"]["value"]
+        if not wl.isolated and run.launches_per_step >= 1 and cfg.chunk_size <= 32:
+            line["mesh_from_occupancy"] = mesh_from_occupancy(ctx, wl, run, stream, flush, args, torch)
+        if cfg.gen.kind in (0, 1):
+            line["noise_kernel"] = noise_kernel(ctx, wl, cfg, stream, flush, args, torch)
+        n_e2e = min(n, 64) if args.workload == "stress" else n
+        faces = run.total_faces if n_e2e == n else int(run.offsets[n_e2e].item())
+        b0, b1 = run.b0, run.b1
+        run.close()
+        torch.cuda.empty_cache()
+        line["e2e"] = e2e_host(ctx, wl, masks, n_e2e, faces, b0, b1, args)
+        if n_e2e < n:
+            line["e2e"]["sample"] = f"first {n_e2e} of {n} chunks"
+        if world == 1 and not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline(wl, cfg, masks, args.cpu_seconds * 0.75)
+            line["cpu_baseline_single_thread"] = cpu_baseline(wl, cfg, masks,
+                                                              args.cpu_seconds * 0.25, threads=1)
+    else:
+        run.close()
+    ctx.close()
+    torch.cuda.empty_cache()
+    if rank == 0 and world == 1 and args.workload == "heightmap" and not args.no_suite:
+        # the other workloads of the suite, each with its own timed region and clocks
+        line["stress"] = sub_workload("stress", args, torch, stream, flush, e2e_chunks=64,
+                                      plain_limit=32)
+        line["density"] = sub_workload("density", args, torch, stream, flush, plain_limit=256)
+        del flush
+        torch.cuda.empty_cache()
+        serving = {"workload": SERVING_TEXT}
+        if args.capacity_chunks > 0:
+            serving["capacity"] = serving_capacity(args.capacity_chunks)
+        if args.serving_frames > 0:
+            serving["paced"] = serving_run(args.serving_frames, paced=True)
+        line["serving"] = serving
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
 
 
 def run_serving(args):
@@ -691,13 +794,11 @@ def run_serving(args):
     frames = args.frames
     res = serving_run(frames, args.paced)
     line = {
-        "metric": METRIC, "value": res["chunks_per_s_busy"], "unit": "chunks/s",
+        "metric": METRIC, "value": res["request_rate_chunks_per_s"], "unit": "chunks/s",
         "n_gpus": 1, "steps": frames, "warmup": 0, "ms_per_step": res["wall_s"] * 1e3 / frames,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32",
         "data": "synthetic",
-        "config": {"workload": "serving: simulated camera 20 u/s + 90 deg/s yaw, 60 frames/s, "
-                               "heightmap-fbm 16^3 chunks, view radius 24, 24 GB LRU cache",
-                   "paced": args.paced},
+        "config": {"workload": SERVING_TEXT, "paced": args.paced},
         "latency": res,
     }
     if rank == 0:

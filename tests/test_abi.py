@@ -28,12 +28,48 @@ def test_header_declares_entry_points():
         assert required in names
 
 
-def test_integration_binding_covers_every_entry_point():
-    """The Rust binding in INTEGRATION.md declares every function of include/*.h."""
-    text = open(os.path.join(REPO, "INTEGRATION.md")).read()
+RUST_BINDING = os.path.join(REPO, "rust", "src", "voxgpu_sys.rs")
+
+
+def test_rust_binding_covers_every_entry_point():
+    """rust/src/voxgpu_sys.rs declares every function of include/*.h, and nothing else."""
+    text = open(RUST_BINDING).read()
     bound = set(re.findall(r"pub fn (vox_\w+)\s*\(", text))
-    missing = [n for n in declared_functions() if n not in bound]
+    declared = declared_functions()
+    missing = [n for n in declared if n not in bound]
     assert not missing, missing
+    assert not (bound - set(declared)), sorted(bound - set(declared))
+
+
+def c_struct_fields():
+    """Field names, in order, of every typedef struct of include/*.h."""
+    out = {}
+    for h in sorted(os.listdir(os.path.join(REPO, "include"))):
+        if not h.endswith(".h"):
+            continue
+        text = re.sub(r"/\*.*?\*/", "", open(os.path.join(REPO, "include", h)).read(), flags=re.S)
+        for body, name in re.findall(r"typedef struct \w+ \{(.*?)\} (\w+);", text, flags=re.S):
+            fields = []
+            for decl in body.split(";"):
+                decl = decl.strip()
+                if not decl:
+                    continue
+                for part in decl.split(","):
+                    m = re.search(r"(\w+)\s*(\[[^\]]*\])*\s*$", part.strip())
+                    fields.append(m.group(1))
+            out[name] = fields
+    return out
+
+
+def test_rust_binding_struct_fields_match_the_headers():
+    text = open(RUST_BINDING).read()
+    rust = {name: re.findall(r"pub (\w+)\s*:", body)
+            for name, body in re.findall(r"pub struct (vox_\w+) \{(.*?)\}", text, flags=re.S)}
+    c = c_struct_fields()
+    assert c, "no structs parsed from the headers"
+    for name, fields in c.items():
+        assert name in rust, name
+        assert rust[name] == fields, (name, rust[name], fields)
 
 
 def test_library_exports_every_declared_symbol(vox):
