@@ -358,12 +358,20 @@ def measure_fused(name, args, torch, stream, flush, world=1, rank=0, local=0, he
         run = BatchRun(ctx, wl.coords, masks, wl.index_base,
                        autotune=not (args.tuning or args.no_autotune), tune_iters=args.tune_iters,
                        graph=not args.no_graph)
+    # nvidia-smi samples every 50 ms, longer than a short timed region: the sampler runs
+    # from the warm-up, which keeps the GPU busy for about 0.3 s, through the timed steps
+    sampler = ClockSampler(local).start()
+    with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             run.launch()
         ctx.sync()
-    sampler = ClockSampler(local).start()
+        t_hold = time.perf_counter()
+        while time.perf_counter() - t_hold < 0.3:
+            for _ in range(8):
+                run.launch()
+            ctx.sync()
     step_ms, wall = timed_steps(run.launch, steps, stream, flush, torch, world)
-    clocks = sampler.stop()
+    clocks = sampler.stop() | {"window": "warm-up (about 0.3 s of replays) through the timed steps"}
     st = ctx.sync(raise_on_error=False)
     assert st == voxgpu.VOX_OK, f"device status {st}"
     n = len(wl.coords)
