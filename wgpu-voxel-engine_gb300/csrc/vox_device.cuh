@@ -361,18 +361,62 @@ __device__ __forceinline__ void halo_coord(int h, int a, int b, int& x, int& y, 
   }
 }
 
+// Threshold of one column (local x, z in -1..N), computed by the calling lane alone: the
+// fBm of the per-column path (d_noise2_axes with the lattice data of this column), then
+// k = ceil(base + amp * fbm) - oy clamped to [-1, N + 1] (-1 for NaN), so that voxel
+// (x, y, z) is solid iff y < k. The same operations, in the same order, as the shared-table
+// path below and as the oracle.
+template <int N, int LAYOUT>
+__device__ __forceinline__ int column_k(const ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox,
+                                        int oy, int oz, int x, int z) {
+  const uint8_t* p = s.tab->perm;
+  const float4* gt = reinterpret_cast<const float4*>(s.tab->grad);
+  float f = g.freq, amp = 1.0f, sum = 0.0f;
+  for (int o = 0; o < g.octaves; ++o) {
+    const float cx = (float)(ox + x) * f, cz = (float)(oz + z) * f;
+    const float flx = floorf(cx), flz = floorf(cz);
+    const int lx = (int)flx & 255;
+    AxisX ax;
+    ax.px = p[lx];
+    ax.px1 = p[lx + 1];
+    ax.fr = cx - flx;
+    ax.u = d_fade(ax.fr);
+    AxisZ az;
+    az.y = (int)flz & 255;
+    az.fr = cz - flz;
+    az.v = d_fade(az.fr);
+    az.pad = 0;
+    sum = sum + amp * d_noise2_axes(p, gt, ax, az);
+    f = f * g.lac;
+    amp = amp * g.gain;
+  }
+  const float h = g.base + g.amp * sum;
+  const float cl = ceilf(h);
+  long long kk = (long long)cl - (long long)oy;
+  if (!(cl == cl)) kk = -1;
+  return (int)(kk < -1 ? -1 : (kk > N + 1 ? N + 1 : kk));
+}
+
 // Heightmap chunk. Column thresholds colk[(z+1)*(N+2) + (x+1)] = ceil(h(x, z)) - oy,
 // clamped to [-1, N + 1], so that voxel (x, y, z), y in [-1, N], is solid iff
 // y < colk (the same as (float)(oy + y) < h for the integer y). The fBm runs octave by
 // octave: the lattice data of every x and z coordinate are computed once per octave,
 // each thread accumulating its own columns in registers.
+//
+// Two ways to the thresholds. The direct path (chunks up to 32^3): every lane of the row
+// phase below computes the threshold of its own column itself, with no shared lattice data,
+// so generation needs no CTA barrier before the row ballots. The shared-table path (larger
+// chunks): the lattice data and corner tables are built once per octave in shared memory,
+// every thread accumulates its columns, and the thresholds go through s.colk.
 template <int N, int LAYOUT, int T>
 __device__ void gen_heightmap(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, int oy, int oz,
                               unsigned halo_mask, bool with_halo) {
   using RowT = typename Shape<N>::RowT;
   constexpr int side = N + 2;
-  constexpr int CPT = (side * side + T - 1) / T;
+  constexpr bool direct = N <= 32;
   const int t = threadIdx.x;
+  if (!direct) {
+  constexpr int CPT = (side * side + T - 1) / T;
   const uint8_t* p = s.tab->perm;
   const float4* gt = reinterpret_cast<const float4*>(s.tab->grad);
   float acc[CPT];
@@ -520,6 +564,7 @@ __device__ void gen_heightmap(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, 
     }
   }
   __syncthreads();
+  }  // !direct
   // Rows from the column thresholds, one warp task per group of columns: the own rows of
   // a group of z values (and their -y / +y halo rows), or one lateral halo strip. Lanes
   // hold one column's threshold k each; rows below the group's smallest k are full, rows
@@ -547,19 +592,28 @@ __device__ void gen_heightmap(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, 
       int rstride;
       if (own) {
         const int z = (task / S) * G + sub;
-        k = s.colk[(z + 1) * side + xb + 1];
+        k = direct ? column_k<N, LAYOUT>(s, g, ox, oy, oz, xb, z) : s.colk[(z + 1) * side + xb + 1];
         base = occw + (task / S) * G * W + seg;
         rstride = N * W;
       } else {
         // lateral halo h: row a = y, bit = position along the strip
         const int c = sub == 0 ? xb : -1;
         active = c >= 0;
-        if (c < 0) k = -1;
-        else if (h == 0) k = s.colk[(c + 1) * side];
-        else if (h == 1) k = s.colk[(c + 1) * side + N + 1];
-        else if (h == 2) k = s.colk[c + 1];
-        else k = s.colk[(N + 1) * side + c + 1];
-        if (!((halo_mask >> h) & 1u) || !with_halo) k = -1;
+        const bool used = ((halo_mask >> h) & 1u) && with_halo;
+        if (c < 0 || !used) {
+          k = -1;
+        } else if (direct) {
+          const int hx = h == 0 ? -1 : (h == 1 ? N : c), hz = h == 2 ? -1 : (h == 3 ? N : c);
+          k = column_k<N, LAYOUT>(s, g, ox, oy, oz, hx, hz);
+        } else if (h == 0) {
+          k = s.colk[(c + 1) * side];
+        } else if (h == 1) {
+          k = s.colk[(c + 1) * side + N + 1];
+        } else if (h == 2) {
+          k = s.colk[c + 1];
+        } else {
+          k = s.colk[(N + 1) * side + c + 1];
+        }
         base = halow + h * N * W + seg;
         rstride = W;
       }
