@@ -103,6 +103,10 @@ def parse_args(argv=None):
     p.add_argument("--frames", type=int, default=10000, help="--workload serving: frames")
     p.add_argument("--paced", action="store_true", help="--workload serving: real-time 60 fps")
     p.add_argument("--tune-iters", type=int, default=5)
+    p.add_argument("--limit-chunks", type=int, default=0,
+                   help="use only the first K chunks of the workload (small cases for profilers)")
+    p.add_argument("--clock-hold", type=float, default=0.3,
+                   help="seconds of untimed replays before the timed steps (clock sampling)")
     return p.parse_args(argv)
 
 
@@ -126,10 +130,18 @@ def shard_workload(wl, rank: int, world: int):
     return voxgpu.Workload(wl.name, wl.cfg_kwargs, coords, wl.index_base, wl.isolated)
 
 
-def config_of(name: str, layout: str):
+def limited(wl, k: int):
+    """The first k chunks of a workload (all of them for k <= 0)."""
+    import voxgpu
+    if k <= 0 or k >= len(wl.coords):
+        return wl
+    return voxgpu.Workload(wl.name, wl.cfg_kwargs, tuple(wl.coords[:k]), wl.index_base, wl.isolated)
+
+
+def config_of(name: str, layout: str, limit: int = 0):
     """The workload description both arms print (the same dict, so the lines compare)."""
     import voxgpu
-    wl = voxgpu.workload(name)
+    wl = limited(voxgpu.workload(name), limit)
     return {"workload": WORKLOAD_TEXT[name], "chunks": len(wl.coords),
             "chunk_size": wl.cfg_kwargs["chunk_size"], "layout": layout}
 
@@ -345,7 +357,7 @@ def measure_fused(name, args, torch, stream, flush, world=1, rank=0, local=0, he
     slab, graph replays timed with events. Returns a dict of figures."""
     import voxgpu
     from voxgpu.batch import BatchRun
-    wl = shard_workload(voxgpu.workload(name), rank, world)
+    wl = shard_workload(limited(voxgpu.workload(name), args.limit_chunks), rank, world)
     layout = voxgpu.LAYOUT_INSTANCED if args.layout == "instanced" else voxgpu.LAYOUT_VERTEX
     cfg = wl.config(layout=layout)
     masks = None if wl.isolated else wl.masks()
@@ -366,12 +378,13 @@ def measure_fused(name, args, torch, stream, flush, world=1, rank=0, local=0, he
             run.launch()
         ctx.sync()
         t_hold = time.perf_counter()
-        while time.perf_counter() - t_hold < 0.3:
+        while time.perf_counter() - t_hold < args.clock_hold:
             for _ in range(8):
                 run.launch()
             ctx.sync()
     step_ms, wall = timed_steps(run.launch, steps, stream, flush, torch, world)
-    clocks = sampler.stop() | {"window": "warm-up (about 0.3 s of replays) through the timed steps"}
+    clocks = sampler.stop() | {"window": f"warm-up ({args.clock_hold:.1f} s of replays) through the "
+                                         "timed steps"}
     st = ctx.sync(raise_on_error=False)
     assert st == voxgpu.VOX_OK, f"device status {st}"
     n = len(wl.coords)
@@ -694,7 +707,7 @@ def sub_workload(name, args, torch, stream, flush, e2e_chunks=None, cpu_seconds=
     path on a prefix and the CPU port on a sample."""
     res, ex = measure_fused(name, args, torch, stream, flush)
     wl, cfg, masks, ctx, run = ex["wl"], ex["cfg"], ex["masks"], ex["ctx"], ex["run"]
-    res["config"] = config_of(name, args.layout)
+    res["config"] = config_of(name, args.layout, args.limit_chunks)
     if plain_limit and args.plain_steps > 0:
         res["plain_per_chunk"] = plain_per_chunk(ctx, wl, cfg, masks, stream, args, torch,
                                                  plain_limit)
@@ -736,7 +749,7 @@ def run_ours(args):
         "steps": res["steps"], "warmup": args.warmup, "ms_per_step": res["ms_per_step"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32+f32",
         "data": "synthetic",
-        "config": config_of(args.workload, args.layout),
+        "config": config_of(args.workload, args.layout, args.limit_chunks),
         "launch": {k: res[k] for k in ("tuning", "launches_per_step", "faces_per_step", "launch",
                                        "l2")} | {"parallelism": f"dp{world} (independent chunk "
                                                                 "batches, no exchange)"},

@@ -147,3 +147,36 @@ def test_slabbed_batch_matches_one_launch_and_reports_capacity(vox, oracle):
         assert np.array_equal(run.out1[:cap * 24].cpu().numpy(), w1)
     run.close()
     ctx.close()
+
+
+@pytest.mark.parametrize("name,limit", [("heightmap", 1024), ("density", 512), ("stress", 16)])
+def test_rank_shards_match_the_oracle(vox, oracle, name, limit):
+    """The weak-scaling shards bench.py gives each rank under torchrun (world size 2):
+    every shard, meshed by the library with the bench's shape, equals the oracle on that
+    shard's own coordinates and chunk indices (ranks run here one after the other; each
+    needs no data from the other)."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    from voxgpu.batch import BatchRun
+    seen = []
+    for rank in (0, 1):
+        wl = bench.shard_workload(vox.workload(name), rank, 2)
+        cfg = wl.config()
+        coords = list(wl.coords)[:limit]
+        masks = None if wl.isolated else vox.neighbour_masks(coords)
+        want_counts, want_dig = oracle.gen_mesh_digests(cfg, coords, masks, wl.index_base)
+        ctx = ctx_for(vox, cfg)
+        run = BatchRun(ctx, coords, masks, wl.index_base, autotune=False)
+        refill_garbage(run)
+        run.launch()
+        ctx.sync()
+        verify_all_chunks(run, oracle, want_counts, want_dig, group=min(len(coords), 256))
+        seen.append((set(coords), wl.index_base))
+        run.close()
+        ctx.close()
+    if name == "stress":
+        assert seen[0][1] != seen[1][1]  # disjoint chunk-index ranges
+    else:
+        assert not (seen[0][0] & seen[1][0])  # disjoint chunk coordinates
