@@ -794,6 +794,69 @@ __device__ __forceinline__ bool dens_solid_tab(const ChunkSmem<N, LAYOUT>& s, co
   return g.solid_below_zero ? (d < 0.0f) : (d > 0.0f);
 }
 
+// The own rows of a 32^3 density chunk from the lattice tables, one row per warp step with
+// lane = x: everything that depends on x alone (the x-axis lattice data of every octave and
+// the corner-table offset of the lane's cell) is read once per chunk into registers, so a
+// sample-octave loads only its y and z axis data and its eight corners. The operations on
+// the values are those of dens_solid_tab, in the same order.
+template <int N, int LAYOUT>
+__device__ __forceinline__ void dens_rows_lane_x(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int oy) {
+  static_assert(N == 32, "lane = x needs 32-voxel rows");
+  const int* hdr = reinterpret_cast<const int*>(s.stage);
+  const DensAxis* axes = reinterpret_cast<const DensAxis*>(s.stage + 64);
+  const float4* corners = reinterpret_cast<const float4*>(s.stage + 64 + kDensMaxOct * 3 * (N + 2) * 16);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  float xf[kDensMaxOct], x1[kDensMaxOct], u[kDensMaxOct];
+  int P[kDensMaxOct], n2[kDensMaxOct], sx[kDensMaxOct];
+#pragma unroll
+  for (int o = 0; o < kDensMaxOct; ++o) {
+    xf[o] = x1[o] = u[o] = 0.0f;
+    P[o] = n2[o] = sx[o] = 0;
+    if (o < g.octaves) {
+      const DensAxis ax = axes[o * 3 * (N + 2) + lane + 1];
+      n2[o] = hdr[4 * o + 2];
+      sx[o] = hdr[4 * o + 1] * n2[o];
+      P[o] = hdr[4 * o] + ax.ci * sx[o];
+      xf[o] = ax.fr;
+      x1[o] = ax.fr1;
+      u[o] = ax.fade;
+    }
+  }
+  uint32_t* occw = reinterpret_cast<uint32_t*>(s.occ);
+  for (int row = warp; row < N * N; row += nwarps) {
+    const int y = row / N, z = row % N;
+    float sum = 0.0f, amp = 1.0f;
+#pragma unroll
+    for (int o = 0; o < kDensMaxOct; ++o) {
+      if (o < g.octaves) {
+        const DensAxis* ao = axes + o * 3 * (N + 2);
+        const DensAxis ay = ao[(N + 2) + y + 1], az = ao[2 * (N + 2) + z + 1];
+        const float4* C = corners + P[o] + ay.ci * n2[o] + az.ci;
+        const int S = sx[o], Z = n2[o];
+        const float4 g000 = C[0], g100 = C[S], g010 = C[Z], g110 = C[S + Z];
+        const float4 g001 = C[1], g101 = C[S + 1], g011 = C[Z + 1], g111 = C[S + Z + 1];
+        const float xx = xf[o], yf = ay.fr, zf = az.fr, xm = x1[o], y1 = ay.fr1, z1 = az.fr1;
+        const float uu = u[o], v = ay.fade, w = az.fade;
+        const float l00 = d_lerp(uu, (g000.x * xx + g000.y * yf) + g000.z * zf,
+                                 (g100.x * xm + g100.y * yf) + g100.z * zf);
+        const float l10 = d_lerp(uu, (g010.x * xx + g010.y * y1) + g010.z * zf,
+                                 (g110.x * xm + g110.y * y1) + g110.z * zf);
+        const float l01 = d_lerp(uu, (g001.x * xx + g001.y * yf) + g001.z * z1,
+                                 (g101.x * xm + g101.y * yf) + g101.z * z1);
+        const float l11 = d_lerp(uu, (g011.x * xx + g011.y * y1) + g011.z * z1,
+                                 (g111.x * xm + g111.y * y1) + g111.z * z1);
+        const float n = d_lerp(w, d_lerp(v, l00, l10), d_lerp(v, l01, l11));
+        sum = sum + amp * n;
+        amp = amp * g.gain;
+      }
+    }
+    const int wy = oy + y;
+    const float d = sum - ((float)wy - g.y_ref) * g.y_scale;
+    const unsigned b = __ballot_sync(0xffffffffu, g.solid_below_zero ? (d < 0.0f) : (d > 0.0f));
+    if (lane == 0) occw[row] = b;
+  }
+}
+
 // Fills s.occ (own rows) and, for every set bit of `halo_mask`, the halo rows; the other
 // halo rows are zero (a neighbour that is not loaded counts as air, chunk.rs:102-107).
 template <int N, int GM, int LAYOUT, int T>
@@ -809,12 +872,16 @@ __device__ void gen_chunk(ChunkSmem<N, LAYOUT>& s, const GenDev& g, vox_chunk_co
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   uint32_t* occw = reinterpret_cast<uint32_t*>(s.occ);
   const bool tab = GM == GM_DENSITY && dens_tables<N, LAYOUT, T>(s, g, ox, oy, oz);
-  for (int base = warp * 32; base < N * N * N; base += nwarps * 32) {
-    const int e = base + lane;
-    const int row = e / N, x = e % N;
-    const int y = row / N, z = row % N;
-    store_ballot<N>(occw, e, tab ? dens_solid_tab<N, LAYOUT>(s, g, x, y, z, oy)
-                                 : gen_solid<N, GM, LAYOUT>(s, g, x, y, z, ox, oy, oz, s0));
+  if (N == 32 && tab) {
+    if constexpr (N == 32) dens_rows_lane_x<N, LAYOUT>(s, g, oy);
+  } else {
+    for (int base = warp * 32; base < N * N * N; base += nwarps * 32) {
+      const int e = base + lane;
+      const int row = e / N, x = e % N;
+      const int y = row / N, z = row % N;
+      store_ballot<N>(occw, e, tab ? dens_solid_tab<N, LAYOUT>(s, g, x, y, z, oy)
+                                   : gen_solid<N, GM, LAYOUT>(s, g, x, y, z, ox, oy, oz, s0));
+    }
   }
   if (with_halo) {
     uint32_t* halow = reinterpret_cast<uint32_t*>(s.halo);
