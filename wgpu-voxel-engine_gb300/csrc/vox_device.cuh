@@ -1126,6 +1126,20 @@ static __device__ unsigned long long lookback(unsigned long long* state, BatchCt
   return excl;
 }
 
+// Pulls the launch's per-chunk inputs (coordinates, neighbour masks) into L2 at the start,
+// one 128-byte line per CTA and step of the grid, so that the chunks' first reads find them
+// there instead of in DRAM.
+__device__ __forceinline__ void prefetch_inputs(const MeshArgs& a) {
+  const unsigned long long cbytes = 12ull * (unsigned long long)a.n;
+  const unsigned long long mbytes = a.nbr_mask ? (unsigned long long)a.n : 0ull;
+  const char* cp = reinterpret_cast<const char*>(a.coords);
+  const char* mp = reinterpret_cast<const char*>(a.nbr_mask);
+  for (unsigned long long off = 128ull * blockIdx.x; off < cbytes; off += 128ull * gridDim.x)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(cp + off));
+  for (unsigned long long off = 128ull * blockIdx.x; off < mbytes; off += 128ull * gridDim.x)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(mp + off));
+}
+
 // Global face index of the launch's first face (MeshArgs::base_ptr; one thread reads it).
 __device__ __forceinline__ unsigned long long launch_base(const MeshArgs& a) {
   return a.base_ptr ? *reinterpret_cast<const volatile unsigned long long*>(a.base_ptr) : 0ull;
@@ -1917,6 +1931,7 @@ k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__
   uint4* const fixed16 = reinterpret_cast<uint4*>(s.occ);  // s.halo, s.rows follow s.occ
   const int t = threadIdx.x;
   if (t == 0) {
+    prefetch_inputs(a);
     s_epoch = ld_relaxed_u32(&a.ctl->epoch);
     s_base0 = launch_base(a);
     __threadfence();
@@ -1960,7 +1975,10 @@ k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__
       prepare_chunk<N, GM, LAYOUT, T>(s, a, i, a.coords[i]);
       const uint32_t total = count_and_scan<N, LAYOUT, T>(s);
       unsigned char* dst = spill + (unsigned long long)i * P::kSpill;
-      for (int q = t; q < kFixed16; q += T) __stcg(reinterpret_cast<uint4*>(dst) + q, fixed16[q]);
+      // an empty chunk (no row with faces) spills only its counts: its emission item
+      // reloads nothing
+      if (s.misc[0] > 0)
+        for (int q = t; q < kFixed16; q += T) __stcg(reinterpret_cast<uint4*>(dst) + q, fixed16[q]);
       const int nzw = (s.misc[0] + 1) >> 1;
       const int vlw = s.misc[1] > 0 ? (s.misc[1] + 1) >> 1 : 0;
       for (int q = t; q < nzw; q += T)
@@ -2000,8 +2018,12 @@ k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__
       constexpr int TR = T > 32 ? T - 32 : 32;  // reloading threads
       const int tr = T > 32 ? t - 32 : t;
       if (t < 32 && ok) {
-        const unsigned long long total = __ldcg(
-            reinterpret_cast<const uint32_t*>(src + P::kOcc + P::kHalo) + Shape<N>::R);
+        // the chunk's face total (an empty chunk spilled only its counts: total 0)
+        const int rows_with_faces = __ldcg(reinterpret_cast<const int*>(src + kMiscOff));
+        const unsigned long long total =
+            rows_with_faces > 0
+                ? __ldcg(reinterpret_cast<const uint32_t*>(src + P::kOcc + P::kHalo) + Shape<N>::R)
+                : 0ull;
         // An inclusive state (chunk 0, or a segment of a chunk whose offset another item
         // has already found) gives the offset at once.
         w = __shfl_sync(0xffffffffu, w, 0);
