@@ -63,7 +63,7 @@ NCU = {
         "traffic": 6473984, "warp_instructions": 16886488, "chunks": 1024,
         "summary": "profiles/k_mesh_batch_phased_heightmap.md"},
     ("k_mesh_batch_overlap", "density"): {
-        "traffic": 683480320, "warp_instructions": 1625252837, "chunks": 4096,
+        "traffic": 660076544, "warp_instructions": 1435145110, "chunks": 4096,
         "summary": "profiles/k_mesh_batch_overlap_density.md"},
     ("k_mesh_batch_overlap", "stress"): {
         "traffic": 47944924160, "chunks": 1024, "scaled_from_chunks": 48,
