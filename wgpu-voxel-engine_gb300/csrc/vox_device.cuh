@@ -416,154 +416,154 @@ __device__ void gen_heightmap(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, 
   constexpr bool direct = N <= 32;
   const int t = threadIdx.x;
   if (!direct) {
-  constexpr int CPT = (side * side + T - 1) / T;
-  const uint8_t* p = s.tab->perm;
-  const float4* gt = reinterpret_cast<const float4*>(s.tab->grad);
-  float acc[CPT];
-#pragma unroll
-  for (int c = 0; c < CPT; ++c) acc[c] = 0.0f;
-  // Corner tables (one octave group, positive frequencies, few enough corners): per octave
-  // the gradient coefficients of every lattice corner the chunk's columns touch. A corner's
-  // hash p[p[p[X] + Y]] depends only on its coordinates mod 256 (the permutation table is
-  // doubled), so a column reads 4 table entries instead of 8 permutation bytes and 4
-  // gradient entries; the arithmetic is the per-column path's, in the same order.
-  bool tab = false;
-  if (g.octaves <= kOctGroup) {
-    if (t < 32) {
-      constexpr int kCap = dens_max_corners<N>();
-      int cnt = 0, ncz = 0, x0 = 0, z0 = 0;
-      bool ok = true;
-      if (t < g.octaves) {
-        float fo = g.freq;
-        for (int q = 0; q < t; ++q) fo = fo * g.lac;
-        // positive, and small enough that every cell index fits an int
-        ok = fo > 0.0f && fabsf((float)(ox - 1) * fo) < 1.0e9f &&
-             fabsf((float)(ox + N) * fo) < 1.0e9f && fabsf((float)(oz - 1) * fo) < 1.0e9f &&
-             fabsf((float)(oz + N) * fo) < 1.0e9f;
-        if (ok) {
-          // coordinates grow with the local index (fo > 0): local -1 has the first cell
-          x0 = (int)floorf((float)(ox - 1) * fo);
-          z0 = (int)floorf((float)(oz - 1) * fo);
-          const int ncx = (int)floorf((float)(ox + N) * fo) - x0 + 2;
-          ncz = (int)floorf((float)(oz + N) * fo) - z0 + 2;
-          ok = ncx > 0 && ncz > 0 && ncx <= kCap && ncz <= kCap && ncx * ncz <= kCap;
-          cnt = ok ? ncx * ncz : 0;
+    constexpr int CPT = (side * side + T - 1) / T;
+    const uint8_t* p = s.tab->perm;
+    const float4* gt = reinterpret_cast<const float4*>(s.tab->grad);
+    float acc[CPT];
+  #pragma unroll
+    for (int c = 0; c < CPT; ++c) acc[c] = 0.0f;
+    // Corner tables (one octave group, positive frequencies, few enough corners): per octave
+    // the gradient coefficients of every lattice corner the chunk's columns touch. A corner's
+    // hash p[p[p[X] + Y]] depends only on its coordinates mod 256 (the permutation table is
+    // doubled), so a column reads 4 table entries instead of 8 permutation bytes and 4
+    // gradient entries; the arithmetic is the per-column path's, in the same order.
+    bool tab = false;
+    if (g.octaves <= kOctGroup) {
+      if (t < 32) {
+        constexpr int kCap = dens_max_corners<N>();
+        int cnt = 0, ncz = 0, x0 = 0, z0 = 0;
+        bool ok = true;
+        if (t < g.octaves) {
+          float fo = g.freq;
+          for (int q = 0; q < t; ++q) fo = fo * g.lac;
+          // positive, and small enough that every cell index fits an int
+          ok = fo > 0.0f && fabsf((float)(ox - 1) * fo) < 1.0e9f &&
+               fabsf((float)(ox + N) * fo) < 1.0e9f && fabsf((float)(oz - 1) * fo) < 1.0e9f &&
+               fabsf((float)(oz + N) * fo) < 1.0e9f;
+          if (ok) {
+            // coordinates grow with the local index (fo > 0): local -1 has the first cell
+            x0 = (int)floorf((float)(ox - 1) * fo);
+            z0 = (int)floorf((float)(oz - 1) * fo);
+            const int ncx = (int)floorf((float)(ox + N) * fo) - x0 + 2;
+            ncz = (int)floorf((float)(oz + N) * fo) - z0 + 2;
+            ok = ncx > 0 && ncz > 0 && ncx <= kCap && ncz <= kCap && ncx * ncz <= kCap;
+            cnt = ok ? ncx * ncz : 0;
+          }
+        }
+        int incl = cnt;
+  #pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const int u = __shfl_up_sync(0xffffffffu, incl, off);
+          if (t >= off) incl += u;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        const bool all_ok = __all_sync(0xffffffffu, ok);
+        if (t < g.octaves) {
+          s.hhdr[4 * t + 0] = incl - cnt;
+          s.hhdr[4 * t + 1] = ncz;
+          s.hhdr[4 * t + 2] = x0;
+          s.hhdr[4 * t + 3] = z0;
+        }
+        if (t == 0) s.hhdr[4 * kOctGroup] = all_ok && total <= kCap ? total : -1;
+      }
+      __syncthreads();
+      tab = s.hhdr[4 * kOctGroup] >= 0;
+    }
+    float f = g.freq, amp = 1.0f;
+    for (int o0 = 0; o0 < g.octaves; o0 += kOctGroup) {
+      const int no = g.octaves - o0 < kOctGroup ? g.octaves - o0 : kOctGroup;
+      // lattice data of every x and z coordinate for the octaves [o0, o0 + no)
+      for (int i = t; i < 2 * side * no; i += T) {
+        const int o = i / (2 * side), r = i % (2 * side);
+        const int a = r / side, k = r % side - 1;
+        float fo = f;
+        for (int q = 0; q < o; ++q) fo = fo * g.lac;
+        const float c = (float)(a == 0 ? ox + k : oz + k) * fo;
+        const float fl = floorf(c);
+        const int L = (int)fl & 255;
+        const float fr = c - fl;
+        if (a == 0) {
+          AxisX v;
+          // tables: the cell relative to the table's first x; else p[X], p[X + 1]
+          v.px = tab ? (int)fl - s.hhdr[4 * o + 2] : p[L];
+          v.px1 = tab ? 0 : p[L + 1];
+          v.fr = fr;
+          v.u = d_fade(fr);
+          s.ax[o * side + k + 1] = v;
+        } else {
+          AxisZ v;
+          v.y = tab ? (int)fl - s.hhdr[4 * o + 3] : L;
+          v.fr = fr;
+          v.v = d_fade(fr);
+          v.pad = 0;
+          s.az[o * side + k + 1] = v;
         }
       }
-      int incl = cnt;
-#pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        const int u = __shfl_up_sync(0xffffffffu, incl, off);
-        if (t >= off) incl += u;
+      if (tab) {
+        const int total = s.hhdr[4 * kOctGroup];
+        for (int i = t; i < total; i += T) {
+          int o = 0;
+          for (int q = 1; q < no; ++q)
+            if (i >= s.hhdr[4 * q]) o = q;
+          const int jj = i - s.hhdr[4 * o], nz = s.hhdr[4 * o + 1];
+          const int X = (s.hhdr[4 * o + 2] + jj / nz) & 255, Y = (s.hhdr[4 * o + 3] + jj % nz) & 255;
+          const float4 gg = gt[p[p[p[X] + Y]] & 15];
+          s.hcorner[i] = make_float2(gg.x, gg.y);
+        }
       }
-      const int total = __shfl_sync(0xffffffffu, incl, 31);
-      const bool all_ok = __all_sync(0xffffffffu, ok);
-      if (t < g.octaves) {
-        s.hhdr[4 * t + 0] = incl - cnt;
-        s.hhdr[4 * t + 1] = ncz;
-        s.hhdr[4 * t + 2] = x0;
-        s.hhdr[4 * t + 3] = z0;
+      __syncthreads();
+  #pragma unroll
+      for (int c = 0; c < CPT; ++c) {
+        const int j = t + c * T;
+        if (j < side * side) {
+          const int zi = j / side, xi = j % side;
+          const bool corner = (zi == 0 || zi == side - 1) && (xi == 0 || xi == side - 1);
+          if (!corner) {
+            float a = amp, sum = acc[c];
+            if (tab) {
+              for (int o = 0; o < no; ++o) {
+                const AxisX ax = s.ax[o * side + xi];
+                const AxisZ az = s.az[o * side + zi];
+                const int nz = s.hhdr[4 * o + 1];
+                const float2* C = s.hcorner + s.hhdr[4 * o] + ax.px * nz + az.y;
+                const float2 g00 = C[0], g01 = C[1], g10 = C[nz], g11 = C[nz + 1];
+                const float x = ax.fr, y = az.fr;
+                const float x1 = x - 1.0f, y1 = y - 1.0f;
+                const float l0 = d_lerp(ax.u, g00.x * x + g00.y * y, g10.x * x1 + g10.y * y);
+                const float l1 = d_lerp(ax.u, g01.x * x + g01.y * y1, g11.x * x1 + g11.y * y1);
+                sum = sum + a * d_lerp(az.v, l0, l1);
+                a = a * g.gain;
+              }
+            } else {
+              for (int o = 0; o < no; ++o) {
+                sum = sum + a * d_noise2_axes(p, gt, s.ax[o * side + xi], s.az[o * side + zi]);
+                a = a * g.gain;
+              }
+            }
+            acc[c] = sum;
+          }
+        }
       }
-      if (t == 0) s.hhdr[4 * kOctGroup] = all_ok && total <= kCap ? total : -1;
+      for (int o = 0; o < no; ++o) {
+        f = f * g.lac;
+        amp = amp * g.gain;
+      }
+      // the next group rewrites the lattice data; after the last group the thresholds
+      // below use only this thread's sums
+      if (o0 + kOctGroup < g.octaves) __syncthreads();
     }
-    __syncthreads();
-    tab = s.hhdr[4 * kOctGroup] >= 0;
-  }
-  float f = g.freq, amp = 1.0f;
-  for (int o0 = 0; o0 < g.octaves; o0 += kOctGroup) {
-    const int no = g.octaves - o0 < kOctGroup ? g.octaves - o0 : kOctGroup;
-    // lattice data of every x and z coordinate for the octaves [o0, o0 + no)
-    for (int i = t; i < 2 * side * no; i += T) {
-      const int o = i / (2 * side), r = i % (2 * side);
-      const int a = r / side, k = r % side - 1;
-      float fo = f;
-      for (int q = 0; q < o; ++q) fo = fo * g.lac;
-      const float c = (float)(a == 0 ? ox + k : oz + k) * fo;
-      const float fl = floorf(c);
-      const int L = (int)fl & 255;
-      const float fr = c - fl;
-      if (a == 0) {
-        AxisX v;
-        // tables: the cell relative to the table's first x; else p[X], p[X + 1]
-        v.px = tab ? (int)fl - s.hhdr[4 * o + 2] : p[L];
-        v.px1 = tab ? 0 : p[L + 1];
-        v.fr = fr;
-        v.u = d_fade(fr);
-        s.ax[o * side + k + 1] = v;
-      } else {
-        AxisZ v;
-        v.y = tab ? (int)fl - s.hhdr[4 * o + 3] : L;
-        v.fr = fr;
-        v.v = d_fade(fr);
-        v.pad = 0;
-        s.az[o * side + k + 1] = v;
-      }
-    }
-    if (tab) {
-      const int total = s.hhdr[4 * kOctGroup];
-      for (int i = t; i < total; i += T) {
-        int o = 0;
-        for (int q = 1; q < no; ++q)
-          if (i >= s.hhdr[4 * q]) o = q;
-        const int jj = i - s.hhdr[4 * o], nz = s.hhdr[4 * o + 1];
-        const int X = (s.hhdr[4 * o + 2] + jj / nz) & 255, Y = (s.hhdr[4 * o + 3] + jj % nz) & 255;
-        const float4 gg = gt[p[p[p[X] + Y]] & 15];
-        s.hcorner[i] = make_float2(gg.x, gg.y);
-      }
-    }
-    __syncthreads();
-#pragma unroll
+  #pragma unroll
     for (int c = 0; c < CPT; ++c) {
       const int j = t + c * T;
       if (j < side * side) {
-        const int zi = j / side, xi = j % side;
-        const bool corner = (zi == 0 || zi == side - 1) && (xi == 0 || xi == side - 1);
-        if (!corner) {
-          float a = amp, sum = acc[c];
-          if (tab) {
-            for (int o = 0; o < no; ++o) {
-              const AxisX ax = s.ax[o * side + xi];
-              const AxisZ az = s.az[o * side + zi];
-              const int nz = s.hhdr[4 * o + 1];
-              const float2* C = s.hcorner + s.hhdr[4 * o] + ax.px * nz + az.y;
-              const float2 g00 = C[0], g01 = C[1], g10 = C[nz], g11 = C[nz + 1];
-              const float x = ax.fr, y = az.fr;
-              const float x1 = x - 1.0f, y1 = y - 1.0f;
-              const float l0 = d_lerp(ax.u, g00.x * x + g00.y * y, g10.x * x1 + g10.y * y);
-              const float l1 = d_lerp(ax.u, g01.x * x + g01.y * y1, g11.x * x1 + g11.y * y1);
-              sum = sum + a * d_lerp(az.v, l0, l1);
-              a = a * g.gain;
-            }
-          } else {
-            for (int o = 0; o < no; ++o) {
-              sum = sum + a * d_noise2_axes(p, gt, s.ax[o * side + xi], s.az[o * side + zi]);
-              a = a * g.gain;
-            }
-          }
-          acc[c] = sum;
-        }
+        const float h = g.base + g.amp * acc[c];
+        const float cl = ceilf(h);
+        long long kk = (long long)cl - (long long)oy;
+        if (!(cl == cl)) kk = -1;
+        s.colk[j] = (int)(kk < -1 ? -1 : (kk > N + 1 ? N + 1 : kk));
       }
     }
-    for (int o = 0; o < no; ++o) {
-      f = f * g.lac;
-      amp = amp * g.gain;
-    }
-    // the next group rewrites the lattice data; after the last group the thresholds
-    // below use only this thread's sums
-    if (o0 + kOctGroup < g.octaves) __syncthreads();
-  }
-#pragma unroll
-  for (int c = 0; c < CPT; ++c) {
-    const int j = t + c * T;
-    if (j < side * side) {
-      const float h = g.base + g.amp * acc[c];
-      const float cl = ceilf(h);
-      long long kk = (long long)cl - (long long)oy;
-      if (!(cl == cl)) kk = -1;
-      s.colk[j] = (int)(kk < -1 ? -1 : (kk > N + 1 ? N + 1 : kk));
-    }
-  }
-  __syncthreads();
+    __syncthreads();
   }  // !direct
   // Rows from the column thresholds, one warp task per group of columns: the own rows of
   // a group of z values (and their -y / +y halo rows), or one lateral halo strip. Lanes
