@@ -180,3 +180,59 @@ def test_rank_shards_match_the_oracle(vox, oracle, name, limit):
         assert seen[0][1] != seen[1][1]  # disjoint chunk-index ranges
     else:
         assert not (seen[0][0] & seen[1][0])  # disjoint chunk coordinates
+
+
+@pytest.mark.parametrize("schedule", [0, 1, 2])
+def test_slabbed_graph_replays(vox, oracle, schedule):
+    """A captured graph holding several slab launches (300-chunk slabs of the 1024-chunk
+    heightmap batch, the last one shorter) replays to the oracle's bytes, twice in a row."""
+    from voxgpu.batch import BatchRun
+    wl = vox.workload("heightmap")
+    cfg = wl.config()
+    coords, masks = list(wl.coords), wl.masks()
+    want_counts, want_dig = oracle.gen_mesh_digests(cfg, coords, masks)
+    ctx = ctx_for(vox, cfg)
+    t = ctx.tuning()
+    ctx.set_tuning(t.threads, t.stage_faces, 0, schedule, 300)
+    run = BatchRun(ctx, coords, masks, graph=True)
+    assert run.launches_per_step == 4
+    for _ in range(2):
+        refill_garbage(run)
+        run.launch()
+        ctx.sync()
+        verify_all_chunks(run, oracle, want_counts, want_dig, group=len(coords))
+    run.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("schedule", [0, 1, 2])
+def test_slabbed_host_entry_point(vox, oracle, schedule):
+    """vox_gen_mesh_host with 64-chunk slabs writes page-locked host buffers in place: the
+    offsets and bytes of one launch, and a short output reports the full offsets."""
+    from gpu_util import Pinned
+    wl = vox.workload("heightmap")
+    cfg = wl.config()
+    n = 200
+    coords = np.asarray(wl.coords[:n], np.int32)
+    masks = np.asarray(vox.neighbour_masks(wl.coords[:n]), np.uint8)
+    w0, w1, woffs = oracle.gen_mesh_batch(cfg, wl.coords[:n], masks)
+    total = int(woffs[-1])
+    ctx = ctx_for(vox, cfg)
+    t = ctx.tuning()
+    ctx.set_tuning(t.threads, t.stage_faces, 0, schedule, 64)
+    hc, hm = Pinned(vox, coords.nbytes), Pinned(vox, masks.nbytes)
+    hc.view(np.int32)[:] = coords.reshape(-1)
+    hm.view(np.uint8)[:] = masks
+    h0, h1, ho = Pinned(vox, total * 96), Pinned(vox, total * 24), Pinned(vox, (n + 1) * 8)
+    for _ in range(2):
+        h0.a.fill(0xEE)
+        ctx.gen_mesh_host(hc.ptr, hm.ptr, n, h0.ptr, h1.ptr, total, ho.ptr)
+        assert np.array_equal(ho.view(np.uint64), woffs)
+        assert np.array_equal(h0.view(np.uint8), w0) and np.array_equal(h1.view(np.uint8), w1)
+    st = ctx.gen_mesh_host(hc.ptr, hm.ptr, n, h0.ptr, h1.ptr, total // 2, ho.ptr,
+                           raise_on_error=False)
+    assert st == vox.VOX_ERR_CAPACITY and np.array_equal(ho.view(np.uint64), woffs)
+    assert np.array_equal(h0.view(np.uint8)[:(total // 2) * 96], w0[:(total // 2) * 96])
+    for b in (hc, hm, h0, h1, ho):
+        b.free()
+    ctx.close()
