@@ -91,8 +91,9 @@ def parse_args(argv=None):
     p.add_argument("--no-graph", action="store_true",
                    help="launch through vox_gen_mesh_batch instead of replaying a captured graph")
     p.add_argument("--tuning", default=None,
-                   help="force a launch shape 'threads,stage_faces,ctas_per_sm[,schedule[,slab]]' "
-                        "(schedule 0 look-back, 1 phased, 2 overlap; no autotune)")
+                   help="force a launch shape 'threads,stage_faces,ctas_per_sm[,schedule[,slab[,halo]]]' "
+                        "(schedule 0 look-back, 1 phased, 2 overlap; halo 0 regenerated, 1 pool; "
+                        "no autotune)")
     p.add_argument("--no-suite", action="store_true",
                    help="headline workload only (no stress / density / serving sub-runs)")
     p.add_argument("--suite-steps", type=int, default=0, help="timed steps of the sub-runs (0: --steps)")
@@ -402,7 +403,10 @@ def measure_fused(name, args, torch, stream, flush, world=1, rank=0, local=0, he
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
     kname = {"phased": "k_mesh_batch_phased", "overlap": "k_mesh_batch_overlap"}.get(
         run.tuning.get("schedule"), "k_mesh_batch")
-    prof = NCU.get((kname, name))
+    staged = run.tuning.get("halo") == "pool"
+    prof = None if staged else NCU.get((kname, name))
+    if staged:  # the step is the staged-halo sequence, the meshing kernel reading the pool
+        kname += " (staged halo: coordinate map, neighbour lookup, k_generate into the pool)"
     roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind,
             "algorithmic_bytes_per_step": alg_bytes, "launches_per_step": launches,
@@ -436,7 +440,10 @@ def measure_fused(name, args, torch, stream, flush, world=1, rank=0, local=0, he
             "frac": instr / (kernel_ms / 1e3) / ISSUE_PEAK,
             "peak_source": "nominal (152 SMs x 4 schedulers x 2.07 GHz); instructions from "
                            + prof["summary"]}
-    noise = noise_report(wl, cfg, masks if masks is not None else [0] * n, ms_per_step)
+    # with staged halos no halo sample is evaluated (every neighbour of these workloads is in
+    # the batch and is read from the pool)
+    noise = noise_report(wl, cfg, masks if masks is not None and not staged else [0] * n,
+                         ms_per_step)
     if noise:
         res["noise_fp32"] = noise
     extras = {"wl": wl, "cfg": cfg, "masks": masks, "ctx": ctx, "run": run}

@@ -251,6 +251,14 @@ typedef struct vox_tuning {
                           consecutive launches of this many chunks, each writing its slab of
                           the output right after the previous one's (same bytes and offsets
                           as one launch); 0 = the whole batch in one launch */
+  int32_t halo_staging;/* 0: each chunk's lateral halo is regenerated in shared memory by the
+                          fused launch; 1: every chunk of the batch (and every loaded
+                          neighbour outside it) is generated once into an occupancy pool, and
+                          the chunks are meshed from the pool with each halo plane read from
+                          the neighbour's occupancy, the neighbours being found by a hash
+                          lookup of the batch's coordinates. Same bytes either way; mode 1
+                          needs chunk coordinates within [-2^20, 2^20) (otherwise
+                          VOX_ERR_INVALID from vox_ctx_sync) */
 } vox_tuning;
 
 /* Schedules of the fused batch kernel (all write the same bytes):
@@ -270,9 +278,10 @@ int vox_ctx_set_tuning(vox_ctx* ctx, const vox_tuning* tuning);
 /* Autotuner: times every candidate launch shape (schedule x CTA size x staging window x
  * CTAs per SM) on the given batch with vox_gen_mesh_batch (same arguments; iters launches each),
  * then, for the fastest shape, the output slab (the whole batch, or halves, quarters and
- * eighths of it while a launch keeps at least two waves of the grid); keeps the fastest in
- * the context and returns it in *out. The outputs of every candidate are identical; the
- * buffers hold the last run's result. */
+ * eighths of it while a launch keeps at least two waves of the grid), then the halo staging
+ * (regenerated or staged from a pool); keeps the fastest in the context and returns it in
+ * *out. The outputs of every candidate are identical; the buffers hold the last run's
+ * result. */
 int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
                  int32_t n, int64_t chunk_index_base, void* d_out0, void* d_out1,
                  uint64_t cap_faces, uint64_t* d_face_offsets, int32_t iters, vox_tuning* out);

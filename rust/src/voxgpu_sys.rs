@@ -25,7 +25,7 @@ use std::os::raw::{c_char, c_int, c_void};
 }
 #[repr(C)] #[derive(Clone, Copy, Default)] pub struct vox_tuning {
     pub threads: i32, pub stage_faces: i32, pub ctas_per_sm: i32, pub schedule: i32,
-    pub slab_chunks: i32,
+    pub slab_chunks: i32, pub halo_staging: i32,
 }
 #[repr(C)] #[derive(Clone, Copy, Default)] pub struct vox_draw_indexed_indirect {
     pub index_count: u32, pub instance_count: u32, pub first_index: u32, pub base_vertex: i32,

@@ -25,6 +25,33 @@ using namespace vox;
 constexpr int kStageSingle = 32;
 constexpr int kStageDouble = 64;
 
+// Buffers of the staged-halo path for batches of up to `cap` chunks (see vox_halo.cu): the
+// coordinate hash map, the neighbour slots, the identity slots, the neighbours outside the
+// batch and their count, and the occupancy pool (cap * (1 + dirs) slots).
+struct HaloScratch {
+  size_t cap = 0;
+  int dirs = 4;
+  unsigned long long* keys = nullptr;
+  int* vals = nullptr;
+  unsigned cap_mask = 0;
+  int* nbr = nullptr;
+  int* ident = nullptr;
+  vox_chunk_coord* extra = nullptr;
+  unsigned* extra_count = nullptr;
+  uint32_t* pool = nullptr;
+
+  void release() {
+    cudaFree(keys);
+    cudaFree(vals);
+    cudaFree(nbr);
+    cudaFree(ident);
+    cudaFree(extra);
+    cudaFree(extra_count);
+    cudaFree(pool);
+    *this = HaloScratch{};
+  }
+};
+
 struct vox_ctx {
   vox_config cfg{};
   int device = 0;
@@ -44,6 +71,8 @@ struct vox_ctx {
   int schedule = VOX_SCHEDULE_LOOKBACK;
   int spin_limit = kSpinLimit;
   int slab_chunks = 0;  // chunks per launch of a batch (0: the whole batch in one launch)
+  int halo_staging = 0; // 0: halos regenerated in the fused launch; 1: staged from a pool
+  HaloScratch halo;     // the staged-halo path's buffers
   int batch_grid[4] = {0, 0, 0, 0};   // persistent grid per gen mode (look-back kernel)
   int phased_grid[4] = {0, 0, 0, 0};  // co-resident grid per gen mode (phased kernel)
   int overlap_grid[4] = {0, 0, 0, 0}; // persistent grid per gen mode (overlap kernel)
@@ -86,6 +115,7 @@ struct vox_graph {
   size_t state_bytes = 0;
   unsigned long long wiped_at = 0;        // context launch count when d_state was zeroed
   int launches = 1;                       // kernel launches per replay (slabs of the batch)
+  HaloScratch halo;                       // staged-halo buffers of the captured batch
 };
 
 namespace {
@@ -184,11 +214,13 @@ int prepare_kernel(vox_ctx* ctx, const void* fn, int smem) {
 
 // Validates a tuning and computes the persistent grid of every generator mode for it.
 int apply_tuning(vox_ctx* ctx, int topt, int stage_faces, int ctas_per_sm, int schedule,
-                 int slab_chunks) {
+                 int slab_chunks, int halo_staging) {
   const KernelSet& ks = *ctx->ks;
   const int layout = ctx->cfg.layout;
   if (topt < 0 || topt > 1) return fail(ctx, VOX_ERR_INVALID, "unsupported CTA size");
   if (slab_chunks < 0) return fail(ctx, VOX_ERR_INVALID, "slab_chunks must be >= 0");
+  if (halo_staging != 0 && halo_staging != 1)
+    return fail(ctx, VOX_ERR_INVALID, "halo_staging must be 0 (regenerate) or 1 (pool)");
   if (stage_faces != 0 && stage_faces != kStageSingle && stage_faces != kStageDouble)
     return fail(ctx, VOX_ERR_INVALID, "stage_faces must be 0 (direct stores), %d or %d",
                 kStageSingle, kStageDouble);
@@ -226,6 +258,7 @@ int apply_tuning(vox_ctx* ctx, int topt, int stage_faces, int ctas_per_sm, int s
   ctx->ctas_per_sm = ctas_per_sm;
   ctx->schedule = schedule;
   ctx->slab_chunks = slab_chunks;
+  ctx->halo_staging = halo_staging;
   for (int gm = 0; gm < 4; ++gm) {
     ctx->batch_grid[gm] = grid[gm];
     ctx->phased_grid[gm] = pgrid[gm];
@@ -386,10 +419,93 @@ int for_each_slab(const MeshArgs& a, int slab, F&& issue) {
   return VOX_OK;
 }
 
+// Staged-halo buffers for batches of n chunks (grow; never shrink).
+int ensure_halo(vox_ctx* ctx, HaloScratch& h, size_t n) {
+  const int dirs = ctx->cfg.cull_mode == VOX_CULL_FULL6 ? 6 : 4;
+  if (n <= h.cap && h.dirs == dirs) return VOX_OK;
+  h.release();
+  const size_t cap = std::max<size_t>(n, 256);
+  size_t slots = 1;
+  while (slots < 2 * cap) slots <<= 1;
+  const size_t words = (size_t)ctx->ks->n_size * ctx->ks->n_size *
+                       (ctx->ks->n_size > 32 ? ctx->ks->n_size / 32 : 1);
+  cudaError_t e;
+  if ((e = cudaMalloc(&h.keys, slots * sizeof(unsigned long long))) != cudaSuccess ||
+      (e = cudaMalloc(&h.vals, slots * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&h.nbr, 6 * cap * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&h.ident, cap * sizeof(int))) != cudaSuccess ||
+      (e = cudaMalloc(&h.extra, (size_t)dirs * cap * sizeof(vox_chunk_coord))) != cudaSuccess ||
+      (e = cudaMalloc(&h.extra_count, sizeof(unsigned))) != cudaSuccess ||
+      (e = cudaMalloc(&h.pool, (1 + (size_t)dirs) * cap * words * sizeof(uint32_t))) != cudaSuccess) {
+    h.release();
+    return cuda_fail(ctx, e, "cudaMalloc(halo staging)");
+  }
+  h.cap = cap;
+  h.dirs = dirs;
+  h.cap_mask = (unsigned)(slots - 1);
+  return VOX_OK;
+}
+
+// The staged-halo pre-pass of a fused batch `a` (generator mode gm): the neighbour lookup,
+// then every chunk of the batch and every loaded neighbour outside it generated into the
+// pool; `a` becomes the equivalent batch over resident occupancy (GM_OCC). The bytes it
+// then writes are the fused launch's: a halo plane read from the neighbour's occupancy is
+// the plane the fused launch generates (generation is a function of the voxel's world
+// position; Bernoulli chunks have no neighbours).
+int halo_prepass(vox_ctx* ctx, MeshArgs& a, int gm, HaloScratch& h, cudaStream_t stream) {
+  const size_t words = (size_t)ctx->ks->n_size * ctx->ks->n_size *
+                       (ctx->ks->n_size > 32 ? ctx->ks->n_size / 32 : 1);
+  HaloLookup hl;
+  hl.coords = a.coords;
+  hl.masks = gm == GM_BERNOULLI ? nullptr : a.nbr_mask;
+  hl.n = a.n;
+  hl.dirs = h.dirs;
+  hl.keys = h.keys;
+  hl.vals = h.vals;
+  hl.cap_mask = h.cap_mask;
+  hl.nbr_slots = h.nbr;
+  hl.ident = h.ident;
+  hl.extra = h.extra;
+  hl.extra_count = h.extra_count;
+  hl.err = &ctx->d_ctl->err;
+  VOX_CUDA(ctx, launch_halo_lookup(hl, stream), "halo lookup");
+  const int gsmem = ctx->ks->smem_total(VOX_LAYOUT_VERTEX, ctx->ks->gen_threads, 0);
+  MeshArgs g = base_args(ctx);
+  g.n = a.n;
+  g.index_base = a.index_base;
+  g.coords = a.coords;
+  uint32_t* own = h.pool;
+  void* p1[] = {&g, &own};
+  VOX_CUDA(ctx, cudaLaunchKernel(ctx->ks->generate[gm], dim3(a.n), dim3(ctx->ks->gen_threads), p1,
+                                 (size_t)gsmem, stream),
+           "generate (pool)");
+  if (hl.masks) {
+    MeshArgs x = base_args(ctx);
+    x.n = h.dirs * a.n;
+    x.coords = h.extra;
+    x.n_dev = h.extra_count;
+    uint32_t* ext = h.pool + (size_t)a.n * words;
+    void* p2[] = {&x, &ext};
+    VOX_CUDA(ctx, cudaLaunchKernel(ctx->ks->generate[gm], dim3(x.n), dim3(ctx->ks->gen_threads), p2,
+                                   (size_t)gsmem, stream),
+             "generate (outside neighbours)");
+  }
+  a.occ_pool = h.pool;
+  a.pool_slots = (1 + h.dirs) * a.n;
+  a.slots = h.ident;
+  a.nbr_slots = h.nbr;
+  return VOX_OK;
+}
+
 // host_out: the outputs are in host memory; the launch stages every warp's faces in one
 // shared-memory buffer and writes them out with plain full-line stores.
 int batch_launch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out = false) {
   int st;
+  if (ctx->halo_staging && gm != GM_OCC) {
+    if ((st = ensure_halo(ctx, ctx->halo, (size_t)a.n)) != VOX_OK) return st;
+    if ((st = halo_prepass(ctx, a, gm, ctx->halo, ctx->stream)) != VOX_OK) return st;
+    gm = GM_OCC;
+  }
   const int slab = slab_of(ctx, a.n);
   if (ctx->schedule != VOX_SCHEDULE_LOOKBACK) {  // the spill slots of phases A and C
     if ((st = ensure_scratch(ctx, (size_t)slab)) != VOX_OK) return st;
@@ -518,8 +634,8 @@ int vox_ctx_create(const vox_config* cfg, void* stream, vox_ctx** out) {
   const int gsmem = ctx->ks->smem_total(VOX_LAYOUT_VERTEX, ctx->ks->gen_threads, 0);
   for (int gm = 1; gm < 4; ++gm)
     if ((st = prepare_kernel(ctx, ctx->ks->generate[gm], gsmem)) != VOX_OK) return cleanup(st);
-  if (apply_tuning(ctx, default_topt(cfg->chunk_size), kStageSingle, 0, kDefaultSchedule, 0) != VOX_OK &&
-      (st = apply_tuning(ctx, 0, 0, 0, kDefaultSchedule, 0)) != VOX_OK)  // no room to stage
+  if (apply_tuning(ctx, default_topt(cfg->chunk_size), kStageSingle, 0, kDefaultSchedule, 0, 0) != VOX_OK &&
+      (st = apply_tuning(ctx, 0, 0, 0, kDefaultSchedule, 0, 0)) != VOX_OK)  // no room to stage
     return cleanup(st);
   ctx->last_error.clear();
   if ((st = ensure_state(ctx, 1024)) != VOX_OK) return cleanup(st);
@@ -540,6 +656,7 @@ int vox_ctx_destroy(vox_ctx* ctx) {
   cudaFree(ctx->d_offsets);
   cudaFree(ctx->d_out0);
   cudaFree(ctx->d_out1);
+  ctx->halo.release();
   if (ctx->h_ctl) cudaFreeHost(ctx->h_ctl);
   if (ctx->h_err_mirror) cudaFreeHost(ctx->h_err_mirror);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -948,6 +1065,7 @@ int vox_ctx_get_tuning(vox_ctx* ctx, vox_tuning* out) {
   out->ctas_per_sm = ctx->ctas_per_sm;
   out->schedule = ctx->schedule;
   out->slab_chunks = ctx->slab_chunks;
+  out->halo_staging = ctx->halo_staging;
   return VOX_OK;
 }
 
@@ -959,7 +1077,8 @@ int vox_ctx_set_tuning(vox_ctx* ctx, const vox_tuning* t) {
     if (ctx->ks->threads[k] == t->threads) topt = k;
   if (topt < 0) return fail(ctx, VOX_ERR_INVALID, "threads must be %d or %d", ctx->ks->threads[0],
                             ctx->ks->threads[1]);
-  return apply_tuning(ctx, topt, t->stage_faces, t->ctas_per_sm, t->schedule, t->slab_chunks);
+  return apply_tuning(ctx, topt, t->stage_faces, t->ctas_per_sm, t->schedule, t->slab_chunks,
+                      t->halo_staging);
 }
 
 int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d_nbr_mask,
@@ -978,9 +1097,9 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
   VOX_CUDA(ctx, cudaEventCreate(&e0), "cudaEventCreate");
   VOX_CUDA(ctx, cudaEventCreate(&e1), "cudaEventCreate");
   const int keep_t = ctx->topt, keep_s = ctx->stage_faces, keep_c = ctx->ctas_per_sm,
-            keep_p = ctx->schedule, keep_l = ctx->slab_chunks;
+            keep_p = ctx->schedule, keep_l = ctx->slab_chunks, keep_h = ctx->halo_staging;
   float best_ms = 1e30f;
-  int best_t = keep_t, best_s = keep_s, best_c = keep_c, best_p = keep_p, best_l = 0;
+  int best_t = keep_t, best_s = keep_s, best_c = keep_c, best_p = keep_p, best_l = 0, best_h = 0;
   auto run = [&]() {
     MeshArgs a = base_args(ctx);
     a.n = n;
@@ -993,7 +1112,7 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
     a.face_offsets = reinterpret_cast<unsigned long long*>(d_face_offsets);
     return batch_launch(ctx, a, ctx->gm);
   };
-  auto time_candidate = [&](int p, int t, int s, int c, int l) -> bool {  // false: stop (error)
+  auto time_candidate = [&](int p, int t, int s, int c, int l, int h) -> bool {  // false: stop
     if ((st = run()) != VOX_OK) return false;
     cudaEventRecord(e0, ctx->stream);
     for (int k = 0; k < iters && st == VOX_OK; ++k) st = run();
@@ -1012,6 +1131,7 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
       best_c = c;
       best_p = p;
       best_l = l;
+      best_h = h;
     }
     return true;
   };
@@ -1022,43 +1142,49 @@ int vox_autotune(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8_t* d
       for (int s : stages) {
         int full_grid = 0;
         for (int c : ctas) {
-          if (apply_tuning(ctx, t, s, c, p, 0) != VOX_OK) continue;
+          if (apply_tuning(ctx, t, s, c, p, 0, 0) != VOX_OK) continue;
           const int g = p == VOX_SCHEDULE_PHASED    ? ctx->phased_grid[ctx->gm]
                         : p == VOX_SCHEDULE_OVERLAP ? ctx->overlap_grid[ctx->gm]
                                                     : ctx->batch_grid[ctx->gm];
           if (c == 0) full_grid = g;
           else if (g >= full_grid) continue;  // same grid as c = 0
-          if (!(go = time_candidate(p, t, s, c, 0))) break;
+          if (!(go = time_candidate(p, t, s, c, 0, 0))) break;
         }
         if (!go) break;
       }
   // 2. the output slab (chunks per launch) for the best shape: halves, quarters and eighths
   // of the batch, while a launch still holds at least two waves of the persistent grid
   // (a smaller slab keeps a launch's spilled chunk state and its output run L2-sized)
-  if (go && apply_tuning(ctx, best_t, best_s, best_c, best_p, 0) == VOX_OK) {
+  if (go && apply_tuning(ctx, best_t, best_s, best_c, best_p, 0, 0) == VOX_OK) {
     const int g = best_p == VOX_SCHEDULE_PHASED    ? ctx->phased_grid[ctx->gm]
                   : best_p == VOX_SCHEDULE_OVERLAP ? ctx->overlap_grid[ctx->gm]
                                                    : ctx->batch_grid[ctx->gm];
     for (int div = 2; div <= 8 && go; div *= 2) {
       const int l = (n + div - 1) / div;
       if (l < 2 * g) break;
-      if (apply_tuning(ctx, best_t, best_s, best_c, best_p, l) != VOX_OK) continue;
-      go = time_candidate(best_p, best_t, best_s, best_c, l);
+      if (apply_tuning(ctx, best_t, best_s, best_c, best_p, l, 0) != VOX_OK) continue;
+      go = time_candidate(best_p, best_t, best_s, best_c, l, 0);
     }
   }
+  // 3. halo staging for the best shape and slab: the halos regenerated in the fused launch
+  // (every candidate above), or every chunk generated once into a pool with the halo planes
+  // read from the neighbours' occupancy
+  if (go && apply_tuning(ctx, best_t, best_s, best_c, best_p, best_l, 1) == VOX_OK)
+    go = time_candidate(best_p, best_t, best_s, best_c, best_l, 1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   ctx->last_error.clear();
-  const int st2 = apply_tuning(ctx, best_t, best_s, best_c, best_p, best_l);
+  const int st2 = apply_tuning(ctx, best_t, best_s, best_c, best_p, best_l, best_h);
   if (st == VOX_OK) st = st2;
   if (st == VOX_OK) st = sync_locked(ctx);
-  if (st != VOX_OK) apply_tuning(ctx, keep_t, keep_s, keep_c, keep_p, keep_l);
+  if (st != VOX_OK) apply_tuning(ctx, keep_t, keep_s, keep_c, keep_p, keep_l, keep_h);
   if (out) {
     out->threads = ctx->ks->threads[ctx->topt];
     out->stage_faces = ctx->stage_faces;
     out->ctas_per_sm = ctx->ctas_per_sm;
     out->schedule = ctx->schedule;
     out->slab_chunks = ctx->slab_chunks;
+    out->halo_staging = ctx->halo_staging;
   }
   return st;
 }
@@ -1082,6 +1208,7 @@ static void graph_free(vox_graph* g) {
   cudaFree(g->d_state);
   cudaFree(g->d_scratch);
   cudaFree(g->d_counts);
+  g->halo.release();
   delete g;
 }
 
@@ -1130,6 +1257,8 @@ int vox_graph_capture(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8
     g->wiped_at = ctx->launches;
     a.state = g->d_state;
   }
+  // the graph owns its staged-halo buffers too (allocated before the capture)
+  if (ctx->halo_staging && (st = ensure_halo(ctx, g->halo, (size_t)n)) != VOX_OK) return bail(st);
   // Capture on a private stream (thread-local mode: other threads' CUDA calls are not
   // affected), then replay on the context's stream.
   cudaStream_t cs = nullptr;
@@ -1139,7 +1268,10 @@ int vox_graph_capture(vox_ctx* ctx, const vox_chunk_coord* d_coords, const uint8
     cudaStreamDestroy(cs);
     return bail(cuda_fail(ctx, e, "cudaStreamBeginCapture"));
   }
-  st = for_each_slab(a, slab, [&](MeshArgs& b) { return issue_batch(ctx, b, ctx->gm, false, cs); });
+  int gm = ctx->gm;
+  if (ctx->halo_staging && (st = halo_prepass(ctx, a, gm, g->halo, cs)) == VOX_OK) gm = GM_OCC;
+  if (st == VOX_OK)
+    st = for_each_slab(a, slab, [&](MeshArgs& b) { return issue_batch(ctx, b, gm, false, cs); });
   cudaGraph_t graph = nullptr;
   e = cudaStreamEndCapture(cs, &graph);
   cudaStreamDestroy(cs);

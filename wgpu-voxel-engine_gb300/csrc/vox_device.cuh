@@ -2111,7 +2111,8 @@ k_mesh_single(MeshArgs a) {
 
 // Chunk::new for n chunks: one CTA per chunk, occupancy rows written to global memory,
 // chunk i at occ_out + i * words, or at slot a.slots[i] of a pool of a.pool_slots slots when
-// a.slots is set (an out-of-range slot writes nothing and latches ERR_BAD_INPUT).
+// a.slots is set (an out-of-range slot writes nothing and latches ERR_BAD_INPUT). With
+// a.n_dev set, only the first *a.n_dev chunks are generated.
 template <int N, int GM, int T>
 __global__ void __launch_bounds__(T)
 k_generate(MeshArgs a, uint32_t* occ_out) {
@@ -2119,6 +2120,7 @@ k_generate(MeshArgs a, uint32_t* occ_out) {
   ChunkSmem<N, VOX_LAYOUT_VERTEX> s;
   s.carve(smem_raw);
   const int i = blockIdx.x;
+  if (a.n_dev && (unsigned)i >= *a.n_dev) return;  // uniform across the CTA
   long long slot = i;
   if (a.slots) {
     slot = a.slots[i];

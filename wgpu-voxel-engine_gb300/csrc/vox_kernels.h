@@ -52,6 +52,27 @@ cudaError_t launch_draw_list(const Planes& planes, const void* coords,
                              const unsigned long long* offs, int n, int extent, int instanced,
                              DrawRecord* out, uint32_t* count, unsigned* err, cudaStream_t st);
 
+// Neighbour lookup of the staged-halo path (vox_halo.cu): a hash map of the batch's
+// coordinates (cap_mask + 1 slots, a power of two at least twice n), then per chunk and
+// direction the pool slot of the neighbour's occupancy (-1: not loaded), with the
+// neighbours that are not in the batch listed in `extra` (count in *extra_count) for slots
+// n, n + 1, ... Out-of-range coordinates latch ERR_BAD_INPUT in *err.
+struct HaloLookup {
+  const vox_chunk_coord* coords;
+  const uint8_t* masks;  // null: no neighbour is loaded
+  int n;
+  int dirs;              // 4 lateral directions, or 6 with VOX_CULL_FULL6
+  unsigned long long* keys;
+  int* vals;
+  unsigned cap_mask;
+  int* nbr_slots;        // 6 per chunk
+  int* ident;            // ident[i] = i (the batch's own pool slots)
+  vox_chunk_coord* extra;
+  unsigned* extra_count;
+  unsigned* err;
+};
+cudaError_t launch_halo_lookup(const HaloLookup& h, cudaStream_t st);
+
 struct BatchCtl;
 // One look-back for chunk 1 of a batch whose chunk 0 never publishes: the wait must give
 // up after spin_limit polls and latch the timeout bit in ctl (the bounded-wait self-test).

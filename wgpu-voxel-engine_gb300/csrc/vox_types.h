@@ -84,6 +84,9 @@ struct MeshArgs {
   // launch of the same stream wrote as its total; every offset and output index of the
   // launch is shifted by it.
   const unsigned long long* base_ptr;
+  // k_generate: the number of chunks to generate is read from device memory (CTAs at or
+  // beyond it return at once), or null to generate all n.
+  const unsigned* n_dev;
 };
 
 }  // namespace vox

@@ -68,14 +68,15 @@ class Sizes(ctypes.Structure):
 class Tuning(ctypes.Structure):
     _fields_ = [("threads", ctypes.c_int32), ("stage_faces", ctypes.c_int32),
                 ("ctas_per_sm", ctypes.c_int32), ("schedule", ctypes.c_int32),
-                ("slab_chunks", ctypes.c_int32)]
+                ("slab_chunks", ctypes.c_int32), ("halo_staging", ctypes.c_int32)]
 
     def as_dict(self):
         return {"threads": self.threads, "stage_faces": self.stage_faces,
                 "ctas_per_sm": self.ctas_per_sm,
                 "schedule": {SCHEDULE_PHASED: "phased", SCHEDULE_OVERLAP: "overlap"}.get(
                     self.schedule, "lookback"),
-                "slab_chunks": self.slab_chunks}
+                "slab_chunks": self.slab_chunks,
+                "halo": "pool" if self.halo_staging else "regenerated"}
 
 
 class ServeConfig(ctypes.Structure):
@@ -350,8 +351,8 @@ class Context:
         return t
 
     def set_tuning(self, threads: int, stage_faces: int, ctas_per_sm: int = 0,
-                   schedule: int = 0, slab_chunks: int = 0):
-        t = Tuning(threads, stage_faces, ctas_per_sm, schedule, slab_chunks)
+                   schedule: int = 0, slab_chunks: int = 0, halo_staging: int = 0):
+        t = Tuning(threads, stage_faces, ctas_per_sm, schedule, slab_chunks, halo_staging)
         self._check(self._lib.vox_ctx_set_tuning(self._h, ctypes.byref(t)), "vox_ctx_set_tuning")
 
     def autotune(self, d_coords, d_nbr_mask, n: int, d_out0, d_out1, cap_faces: int, d_offsets,
