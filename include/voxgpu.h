@@ -258,7 +258,9 @@ typedef struct vox_tuning {
                           the neighbour's occupancy, the neighbours being found by a hash
                           lookup of the batch's coordinates. Same bytes either way; mode 1
                           needs chunk coordinates within [-2^20, 2^20) (otherwise
-                          VOX_ERR_INVALID from vox_ctx_sync) */
+                          VOX_ERR_INVALID from vox_ctx_sync) and applies to outputs in device
+                          memory: vox_gen_mesh_host with page-locked outputs keeps mode 0,
+                          whose emission overlaps generation behind the host link */
 } vox_tuning;
 
 /* Schedules of the fused batch kernel (all write the same bytes):

@@ -83,6 +83,8 @@ def test_pool_bernoulli_and_plain(vox, oracle):
 
 
 def test_pool_host_entry_point(vox, oracle):
+    """A context tuned to staged halos, through vox_gen_mesh_host: page-locked outputs keep
+    the fused launch, pageable ones go through device buffers and the staged path."""
     wl = vox.workload("heightmap")
     cfg = wl.config()
     n = 200

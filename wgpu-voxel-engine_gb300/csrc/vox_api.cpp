@@ -501,7 +501,9 @@ int halo_prepass(vox_ctx* ctx, MeshArgs& a, int gm, HaloScratch& h, cudaStream_t
 // shared-memory buffer and writes them out with plain full-line stores.
 int batch_launch(vox_ctx* ctx, MeshArgs& a, int gm, bool host_out = false) {
   int st;
-  if (ctx->halo_staging && gm != GM_OCC) {
+  // Outputs in host memory keep the fused launch: its emission, bound by the host link,
+  // overlaps the generation, which the staged-halo path runs first.
+  if (ctx->halo_staging && gm != GM_OCC && !host_out) {
     if ((st = ensure_halo(ctx, ctx->halo, (size_t)a.n)) != VOX_OK) return st;
     if ((st = halo_prepass(ctx, a, gm, ctx->halo, ctx->stream)) != VOX_OK) return st;
     gm = GM_OCC;
