@@ -486,8 +486,10 @@ int halo_prepass(vox_ctx* ctx, MeshArgs& a, int gm, HaloScratch& h, cudaStream_t
     x.n_dev = h.extra_count;
     uint32_t* ext = h.pool + (size_t)a.n * words;
     void* p2[] = {&x, &ext};
-    VOX_CUDA(ctx, cudaLaunchKernel(ctx->ks->generate[gm], dim3(x.n), dim3(ctx->ks->gen_threads), p2,
-                                   (size_t)gsmem, stream),
+    // the count is known on the device only: a grid of 2 CTAs per SM loops over it
+    const int grid = std::max(1, std::min(x.n, 2 * ctx->num_sms));
+    VOX_CUDA(ctx, cudaLaunchKernel(ctx->ks->generate_count[gm], dim3(grid), dim3(ctx->ks->gen_threads),
+                                   p2, (size_t)gsmem, stream),
              "generate (outside neighbours)");
   }
   a.occ_pool = h.pool;
@@ -635,7 +637,9 @@ int vox_ctx_create(const vox_config* cfg, void* stream, vox_ctx** out) {
       return cleanup(st);
   const int gsmem = ctx->ks->smem_total(VOX_LAYOUT_VERTEX, ctx->ks->gen_threads, 0);
   for (int gm = 1; gm < 4; ++gm)
-    if ((st = prepare_kernel(ctx, ctx->ks->generate[gm], gsmem)) != VOX_OK) return cleanup(st);
+    if ((st = prepare_kernel(ctx, ctx->ks->generate[gm], gsmem)) != VOX_OK ||
+        (st = prepare_kernel(ctx, ctx->ks->generate_count[gm], gsmem)) != VOX_OK)
+      return cleanup(st);
   if (apply_tuning(ctx, default_topt(cfg->chunk_size), kStageSingle, 0, kDefaultSchedule, 0, 0) != VOX_OK &&
       (st = apply_tuning(ctx, 0, 0, 0, kDefaultSchedule, 0, 0)) != VOX_OK)  // no room to stage
     return cleanup(st);

@@ -2109,33 +2109,48 @@ k_mesh_single(MeshArgs a) {
   if ((threadIdx.x & 31) == 0) bulk_wait_all();
 }
 
-// Chunk::new for n chunks: one CTA per chunk, occupancy rows written to global memory,
+// Chunk::new for n chunks, occupancy rows written to global memory. One CTA per chunk:
 // chunk i at occ_out + i * words, or at slot a.slots[i] of a pool of a.pool_slots slots when
-// a.slots is set (an out-of-range slot writes nothing and latches ERR_BAD_INPUT). With
-// a.n_dev set, only the first *a.n_dev chunks are generated.
-template <int N, int GM, int T>
+// a.slots is set (an out-of-range slot writes nothing and latches ERR_BAD_INPUT). With LOOP:
+// chunks blockIdx.x, + gridDim.x, ... below the count *a.n_dev read from device memory (at
+// most a.n), each at occ_out + i * words; a grid of a few CTAs per SM then serves any count
+// and costs one check per CTA when there is nothing to generate.
+template <int N, int GM, int T, bool LOOP>
 __global__ void __launch_bounds__(T)
 k_generate(MeshArgs a, uint32_t* occ_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ChunkSmem<N, VOX_LAYOUT_VERTEX> s;
   s.carve(smem_raw);
-  const int i = blockIdx.x;
-  if (a.n_dev && (unsigned)i >= *a.n_dev) return;  // uniform across the CTA
-  long long slot = i;
-  if (a.slots) {
-    slot = a.slots[i];
-    if (slot < 0 || slot >= a.pool_slots) {
-      if (threadIdx.x == 0) atomicOr(&a.ctl->err, ERR_BAD_INPUT);
-      return;  // uniform across the CTA: no barrier has been reached yet
-    }
-  }
-  load_tables<N, VOX_LAYOUT_VERTEX>(s, a.tables);
-  __syncthreads();
-  gen_chunk<N, GM, VOX_LAYOUT_VERTEX, T>(s, a.gen, a.coords[i], a.index_base + i, 0u, false);
   constexpr int words = N * N * Shape<N>::W;
-  const uint32_t* src = reinterpret_cast<const uint32_t*>(s.occ);
-  uint32_t* dst = occ_out + (size_t)slot * words;
-  for (int q = threadIdx.x; q < words; q += blockDim.x) dst[q] = src[q];
+  if constexpr (LOOP) {
+    const int count = (int)min((unsigned)a.n, *a.n_dev);
+    if ((int)blockIdx.x >= count) return;  // uniform across the CTA
+    load_tables<N, VOX_LAYOUT_VERTEX>(s, a.tables);
+    __syncthreads();
+    for (int i = blockIdx.x; i < count; i += gridDim.x) {
+      gen_chunk<N, GM, VOX_LAYOUT_VERTEX, T>(s, a.gen, a.coords[i], a.index_base + i, 0u, false);
+      const uint32_t* src = reinterpret_cast<const uint32_t*>(s.occ);
+      uint32_t* dst = occ_out + (size_t)i * words;
+      for (int q = threadIdx.x; q < words; q += blockDim.x) dst[q] = src[q];
+      __syncthreads();  // the next chunk rewrites s.occ
+    }
+  } else {
+    const int i = blockIdx.x;
+    long long slot = i;
+    if (a.slots) {
+      slot = a.slots[i];
+      if (slot < 0 || slot >= a.pool_slots) {
+        if (threadIdx.x == 0) atomicOr(&a.ctl->err, ERR_BAD_INPUT);
+        return;  // uniform across the CTA: no barrier has been reached yet
+      }
+    }
+    load_tables<N, VOX_LAYOUT_VERTEX>(s, a.tables);
+    __syncthreads();
+    gen_chunk<N, GM, VOX_LAYOUT_VERTEX, T>(s, a.gen, a.coords[i], a.index_base + i, 0u, false);
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(s.occ);
+    uint32_t* dst = occ_out + (size_t)slot * words;
+    for (int q = threadIdx.x; q < words; q += blockDim.x) dst[q] = src[q];
+  }
 }
 
 }  // namespace vox

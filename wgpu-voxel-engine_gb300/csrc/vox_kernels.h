@@ -15,6 +15,7 @@ struct KernelSet {
   const void* overlap[4][2][2]; // k_mesh_batch_overlap<N, gen mode, layout, threads[t]>
   const void* single[2][2];     // k_mesh_single<N, layout, threads[t]>
   const void* generate[4];      // k_generate<N, gen mode, gen_threads> (index 0 unused)
+  const void* generate_count[4];// the same, the chunk count read from device memory
   int gen_threads;
   int spill_bytes;              // chunk state of one chunk (phased scratch)
   // dynamic shared memory of a launch (layout, CTA size, staging window in faces)
