@@ -1,7 +1,7 @@
 """The staged-halo path (vox_tuning.halo_staging = 1) against the oracle, bit for bit.
 
-Every chunk of the batch and every loaded neighbour outside it is generated once into an
-occupancy pool; the neighbours are found by a device hash lookup of the batch's
+Every chunk of the batch is generated once into an occupancy pool, and for every loaded
+neighbour outside it the one plane that the meshing reads; the neighbours are found by a device hash lookup of the batch's
 coordinates, and the chunks are meshed from the pool with each halo plane read from the
 neighbour's occupancy. The bytes must be those of the fused launch, which regenerates the
 halos, and of the oracle, which generates every neighbour from its coordinate.
@@ -59,6 +59,40 @@ def test_pool_density_with_neighbours_outside_the_batch(vox, oracle, cull):
     run.launch()
     ctx.sync()
     verify_all_chunks(run, oracle, want_counts, want_dig, group=len(coords))
+    run.close()
+    ctx.close()
+
+
+@pytest.mark.parametrize("name,size", [("heightmap", 16), ("heightmap", 32), ("heightmap", 64),
+                                       ("density", 8), ("density", 16), ("density", 64)])
+@pytest.mark.parametrize("cull", [0, 1])
+def test_pool_halo_planes_outside_the_batch(vox, oracle, name, size, cull):
+    """Both noise generators at several chunk sizes, every neighbour claimed loaded: each
+    chunk on the block's faces reads its halo from a plane generated alone into an extra
+    pool slot (x, z and, with full culling, y planes on either side)."""
+    from voxgpu.batch import BatchRun
+    wl = vox.workload(name)
+    cfg = vox.Workload(name, dict(wl.cfg_kwargs, chunk_size=size), ()).config(cull_mode=cull)
+    # a block straddling the heightmap's surface (chunk y -1..1) or the density field's
+    # (voxel y 224..319)
+    if name == "heightmap":
+        coords = vox.grid_coords(range(-2, 1), range(-1, 2), range(3, 5))
+    else:
+        ys = range(224 // size, max(320 // size, 224 // size + 2))
+        coords = vox.grid_coords(range(128 // size, 128 // size + 3), ys,
+                                 range(160 // size, 160 // size + 2))
+    masks = [0x3F if cull else 0x0F] * len(coords)
+    want_counts, want_dig = oracle.gen_mesh_digests(cfg, coords, masks)
+    assert sum(want_counts) > 0
+    ctx = ctx_for(vox, cfg)
+    pool_tuning(ctx, 2)
+    run = BatchRun(ctx, coords, masks, graph=False)
+    assert run.tuning["halo"] == "pool"
+    for _ in range(2):
+        refill_garbage(run)
+        run.launch()
+        ctx.sync()
+        verify_all_chunks(run, oracle, want_counts, want_dig, group=len(coords))
     run.close()
     ctx.close()
 

@@ -37,6 +37,7 @@ struct HaloScratch {
   int* nbr = nullptr;
   int* ident = nullptr;
   vox_chunk_coord* extra = nullptr;
+  uint8_t* extra_dir = nullptr;
   unsigned* extra_count = nullptr;
   uint32_t* pool = nullptr;
 
@@ -46,6 +47,7 @@ struct HaloScratch {
     cudaFree(nbr);
     cudaFree(ident);
     cudaFree(extra);
+    cudaFree(extra_dir);
     cudaFree(extra_count);
     cudaFree(pool);
     *this = HaloScratch{};
@@ -435,6 +437,7 @@ int ensure_halo(vox_ctx* ctx, HaloScratch& h, size_t n) {
       (e = cudaMalloc(&h.nbr, 6 * cap * sizeof(int))) != cudaSuccess ||
       (e = cudaMalloc(&h.ident, cap * sizeof(int))) != cudaSuccess ||
       (e = cudaMalloc(&h.extra, (size_t)dirs * cap * sizeof(vox_chunk_coord))) != cudaSuccess ||
+      (e = cudaMalloc(&h.extra_dir, (size_t)dirs * cap)) != cudaSuccess ||
       (e = cudaMalloc(&h.extra_count, sizeof(unsigned))) != cudaSuccess ||
       (e = cudaMalloc(&h.pool, (1 + (size_t)dirs) * cap * words * sizeof(uint32_t))) != cudaSuccess) {
     h.release();
@@ -447,8 +450,8 @@ int ensure_halo(vox_ctx* ctx, HaloScratch& h, size_t n) {
 }
 
 // The staged-halo pre-pass of a fused batch `a` (generator mode gm): the neighbour lookup,
-// then every chunk of the batch and every loaded neighbour outside it generated into the
-// pool; `a` becomes the equivalent batch over resident occupancy (GM_OCC). The bytes it
+// then every chunk of the batch generated into the pool, and for every loaded neighbour
+// outside it the one plane its batch neighbour reads; `a` becomes the equivalent batch over resident occupancy (GM_OCC). The bytes it
 // then writes are the fused launch's: a halo plane read from the neighbour's occupancy is
 // the plane the fused launch generates (generation is a function of the voxel's world
 // position; Bernoulli chunks have no neighbours).
@@ -466,6 +469,7 @@ int halo_prepass(vox_ctx* ctx, MeshArgs& a, int gm, HaloScratch& h, cudaStream_t
   hl.nbr_slots = h.nbr;
   hl.ident = h.ident;
   hl.extra = h.extra;
+  hl.extra_dir = h.extra_dir;
   hl.extra_count = h.extra_count;
   hl.err = &ctx->d_ctl->err;
   VOX_CUDA(ctx, launch_halo_lookup(hl, stream), "halo lookup");
@@ -484,13 +488,14 @@ int halo_prepass(vox_ctx* ctx, MeshArgs& a, int gm, HaloScratch& h, cudaStream_t
     x.n = h.dirs * a.n;
     x.coords = h.extra;
     x.n_dev = h.extra_count;
+    const uint8_t* xdir = h.extra_dir;
     uint32_t* ext = h.pool + (size_t)a.n * words;
-    void* p2[] = {&x, &ext};
+    void* p2[] = {&x, &xdir, &ext};
     // the count is known on the device only: a grid of 2 CTAs per SM loops over it
     const int grid = std::max(1, std::min(x.n, 2 * ctx->num_sms));
-    VOX_CUDA(ctx, cudaLaunchKernel(ctx->ks->generate_count[gm], dim3(grid), dim3(ctx->ks->gen_threads),
+    VOX_CUDA(ctx, cudaLaunchKernel(ctx->ks->generate_planes[gm], dim3(grid), dim3(ctx->ks->gen_threads),
                                    p2, (size_t)gsmem, stream),
-             "generate (outside neighbours)");
+             "generate (halo planes outside the batch)");
   }
   a.occ_pool = h.pool;
   a.pool_slots = (1 + h.dirs) * a.n;
@@ -638,7 +643,8 @@ int vox_ctx_create(const vox_config* cfg, void* stream, vox_ctx** out) {
   const int gsmem = ctx->ks->smem_total(VOX_LAYOUT_VERTEX, ctx->ks->gen_threads, 0);
   for (int gm = 1; gm < 4; ++gm)
     if ((st = prepare_kernel(ctx, ctx->ks->generate[gm], gsmem)) != VOX_OK ||
-        (st = prepare_kernel(ctx, ctx->ks->generate_count[gm], gsmem)) != VOX_OK)
+        (ctx->ks->generate_planes[gm] &&
+         (st = prepare_kernel(ctx, ctx->ks->generate_planes[gm], gsmem)) != VOX_OK))
       return cleanup(st);
   if (apply_tuning(ctx, default_topt(cfg->chunk_size), kStageSingle, 0, kDefaultSchedule, 0, 0) != VOX_OK &&
       (st = apply_tuning(ctx, 0, 0, 0, kDefaultSchedule, 0, 0)) != VOX_OK)  // no room to stage

@@ -73,9 +73,25 @@ struct DensAxis {
 constexpr int kDensMaxOct = 4;
 template <int N>
 __host__ __device__ constexpr int dens_max_corners() { return N <= 8 ? 128 : (N <= 16 ? 256 : 1024); }
+// Byte offsets of the density tables in the generation scratch: int hdr[16] (per octave:
+// corner-table base, corners along y and along z), DensAxis axes[octave][axis][N + 2],
+// for 32^3 chunks the packed x and y records of the lane = z path (two 16-byte records
+// per octave and coordinate), then the corner-pair records: record i holds the gradients
+// of corner i and of corner i + 1 (its +z neighbour on the lattice) as
+// {gx_i, gx_i+1, gy_i, gy_i+1} and {gz_i, gz_i+1}.
+template <int N>
+struct DensPlan {
+  static constexpr bool kLaneZ = N == 32;
+  static constexpr int kAxes = 64;
+  static constexpr int kPackX = kAxes + kDensMaxOct * 3 * (N + 2) * 16;
+  static constexpr int kPackY = kPackX + (kLaneZ ? kDensMaxOct * (N + 2) * 32 : 0);
+  static constexpr int kPairXY = kPackY + (kLaneZ ? kDensMaxOct * (N + 2) * 32 : 0);
+  static constexpr int kPairZ = kPairXY + dens_max_corners<N>() * 16;
+  static constexpr int kBytes = kPairZ + dens_max_corners<N>() * 8;
+};
 template <int N>
 __host__ __device__ constexpr int dens_scratch_bytes() {
-  return 64 + kDensMaxOct * 3 * (N + 2) * 16 + dens_max_corners<N>() * 16;
+  return DensPlan<N>::kBytes;
 }
 // A warp's face list: the faces of one group of 32 voxels (6 each) after fewer than one
 // batch of faces carried over from the previous group.
@@ -138,6 +154,39 @@ __device__ __forceinline__ float d_fade(float t) {
   return t * t * t * (t * (t * 6.0f - 15.0f) + 10.0f);
 }
 __device__ __forceinline__ float d_lerp(float t, float a, float b) { return a + t * (b - a); }
+
+// Packed FP32 pairs: one f32x2 instruction performs the operation on both halves, each
+// rounded to nearest like the scalar add / sub / mul, so a pair of scalar expressions
+// evaluated this way gives the same bits with half the instructions. The low half is the
+// first element.
+typedef unsigned long long f2_t;
+__device__ __forceinline__ f2_t f2_pack(float lo, float hi) {
+  f2_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(f2_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f2_t f2_add(f2_t a, f2_t b) {
+  f2_t r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2_t f2_sub(f2_t a, f2_t b) {
+  f2_t r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2_t f2_mul(f2_t a, f2_t b) {
+  f2_t r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+// d_lerp on both halves
+__device__ __forceinline__ f2_t f2_lerp(f2_t t, f2_t a, f2_t b) {
+  return f2_add(a, f2_mul(t, f2_sub(b, a)));
+}
 // Gradient dot products from the coefficient table (gx, gy, gz) of hash & 15.
 __device__ __forceinline__ float d_grad3(const float4* gt, int h, float x, float y, float z) {
   const float4 g = gt[h & 15];
@@ -668,15 +717,16 @@ __device__ __forceinline__ bool gen_solid(const ChunkSmem<N, LAYOUT>& s, const G
 
 // Builds the density lattice tables of a chunk in the generation scratch (all threads; ends
 // with a barrier) and returns true, or returns false without a barrier when the
-// configuration is beyond the table limits (the same answer in every thread).
-// Scratch layout: int hdr[16] (per octave: corner-table base, corners along y and along
-// z), DensAxis axes[octave][axis][N + 2], float4 corners[...].
+// configuration is beyond the table limits (the same answer in every thread). The layout
+// is DensPlan's.
 template <int N, int LAYOUT, int T>
 __device__ bool dens_tables(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, int oy, int oz) {
+  using P = DensPlan<N>;
   if (g.octaves > kDensMaxOct) return false;
   int* hdr = reinterpret_cast<int*>(s.stage);
-  DensAxis* axes = reinterpret_cast<DensAxis*>(s.stage + 64);
-  float4* corners = reinterpret_cast<float4*>(s.stage + 64 + kDensMaxOct * 3 * (N + 2) * 16);
+  DensAxis* axes = reinterpret_cast<DensAxis*>(s.stage + P::kAxes);
+  uint4* pair_xy = reinterpret_cast<uint4*>(s.stage + P::kPairXY);
+  uint2* pair_z = reinterpret_cast<uint2*>(s.stage + P::kPairZ);
   const int org[3] = {ox, oy, oz};
   // corner counts (every thread computes them; cheap)
   int lo[kDensMaxOct][3], nc[kDensMaxOct][3], base[kDensMaxOct];
@@ -718,14 +768,30 @@ __device__ bool dens_tables(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, in
     v.fr = c - fl;
     v.fade = d_fade(v.fr);
     v.fr1 = v.fr - 1.0f;
-    int c0 = 0;
+    int c0 = 0, n1 = 0, n2 = 0;
 #pragma unroll
-    for (int q = 0; q < kDensMaxOct; ++q)
+    for (int q = 0; q < kDensMaxOct; ++q) {
 #pragma unroll
       for (int b = 0; b < 3; ++b)
         if (q == o && b == a) c0 = lo[q][b];
+      if (q == o) {
+        n1 = nc[q][1];
+        n2 = nc[q][2];
+      }
+    }
     v.ci = (int)fl - c0;
     axes[i] = v;
+    if (P::kLaneZ && a < 2) {
+      // packed x (a = 0) or y (a = 1) record of the lane = z path: {fr, fr, fr1, fr1} and
+      // {fade, fade, offset of cell ci, offset of cell ci + 1} in corner-record units
+      const int stride = a == 0 ? n1 * n2 : n2;
+      uint4* rec = reinterpret_cast<uint4*>(s.stage + (a == 0 ? P::kPackX : P::kPackY)) +
+                   2 * (o * (N + 2) + k);
+      rec[0] = make_uint4(__float_as_uint(v.fr), __float_as_uint(v.fr), __float_as_uint(v.fr1),
+                          __float_as_uint(v.fr1));
+      rec[1] = make_uint4(__float_as_uint(v.fade), __float_as_uint(v.fade),
+                          (unsigned)(v.ci * stride), (unsigned)((v.ci + 1) * stride));
+    }
   }
   // corner gradients: hash p[p[p[X] + Y] + Z] of the corner's lattice coordinates mod 256
   // (the doubled permutation makes this the hash the per-sample chain computes)
@@ -752,7 +818,12 @@ __device__ bool dens_tables(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, in
     iy = (j / n2) % n1;
     ix = j / (n1 * n2);
     const int X = (l0 + ix) & 255, Y = (l1 + iy) & 255, Z = (l2 + iz) & 255;
-    corners[i] = gt[p[p[p[X] + Y] + Z] & 15];
+    // corner i and its +z neighbour (the record of a chunk's last z corner is never read)
+    const float4 g0 = gt[p[p[p[X] + Y] + Z] & 15];
+    const float4 g1 = gt[p[p[p[X] + Y] + ((Z + 1) & 255)] & 15];
+    pair_xy[i] = make_uint4(__float_as_uint(g0.x), __float_as_uint(g1.x), __float_as_uint(g0.y),
+                            __float_as_uint(g1.y));
+    pair_z[i] = make_uint2(__float_as_uint(g0.z), __float_as_uint(g1.z));
   }
   __syncthreads();
   return true;
@@ -763,18 +834,27 @@ __device__ bool dens_tables(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int ox, in
 template <int N, int LAYOUT>
 __device__ __forceinline__ bool dens_solid_tab(const ChunkSmem<N, LAYOUT>& s, const GenDev& g,
                                                int x, int y, int z, int oy) {
+  using P = DensPlan<N>;
   const int* hdr = reinterpret_cast<const int*>(s.stage);
-  const DensAxis* axes = reinterpret_cast<const DensAxis*>(s.stage + 64);
-  const float4* corners = reinterpret_cast<const float4*>(s.stage + 64 + kDensMaxOct * 3 * (N + 2) * 16);
+  const DensAxis* axes = reinterpret_cast<const DensAxis*>(s.stage + P::kAxes);
+  const float4* pair_xy = reinterpret_cast<const float4*>(s.stage + P::kPairXY);
+  const float2* pair_z = reinterpret_cast<const float2*>(s.stage + P::kPairZ);
   float sum = 0.0f, amp = 1.0f;
   for (int o = 0; o < g.octaves; ++o) {
     const DensAxis* ao = axes + o * 3 * (N + 2);
     const DensAxis ax = ao[x + 1], ay = ao[(N + 2) + y + 1], az = ao[2 * (N + 2) + z + 1];
     const int n1 = hdr[4 * o + 1], n2 = hdr[4 * o + 2];
     const int sx = n1 * n2;
-    const float4* C = corners + hdr[4 * o] + (ax.ci * n1 + ay.ci) * n2 + az.ci;
-    const float4 g000 = C[0], g100 = C[sx], g010 = C[n2], g110 = C[sx + n2];
-    const float4 g001 = C[1], g101 = C[sx + 1], g011 = C[n2 + 1], g111 = C[sx + n2 + 1];
+    // the pair records of the four (x, y) corner columns: corners z and z + 1
+    const int c = hdr[4 * o] + (ax.ci * n1 + ay.ci) * n2 + az.ci;
+    const float4 q00 = pair_xy[c], q10 = pair_xy[c + sx], q01 = pair_xy[c + n2],
+                 q11 = pair_xy[c + sx + n2];
+    const float2 h00 = pair_z[c], h10 = pair_z[c + sx], h01 = pair_z[c + n2],
+                 h11 = pair_z[c + sx + n2];
+    const float3 g000 = make_float3(q00.x, q00.z, h00.x), g001 = make_float3(q00.y, q00.w, h00.y);
+    const float3 g100 = make_float3(q10.x, q10.z, h10.x), g101 = make_float3(q10.y, q10.w, h10.y);
+    const float3 g010 = make_float3(q01.x, q01.z, h01.x), g011 = make_float3(q01.y, q01.w, h01.y);
+    const float3 g110 = make_float3(q11.x, q11.z, h11.x), g111 = make_float3(q11.y, q11.w, h11.y);
     const float xf = ax.fr, yf = ay.fr, zf = az.fr, x1 = ax.fr1, y1 = ay.fr1, z1 = az.fr1;
     const float u = ax.fade, v = ay.fade, w = az.fade;
     const float l00 = d_lerp(u, (g000.x * xf + g000.y * yf) + g000.z * zf,
@@ -794,66 +874,91 @@ __device__ __forceinline__ bool dens_solid_tab(const ChunkSmem<N, LAYOUT>& s, co
   return g.solid_below_zero ? (d < 0.0f) : (d > 0.0f);
 }
 
-// The own rows of a 32^3 density chunk from the lattice tables, one row per warp step with
-// lane = x: everything that depends on x alone (the x-axis lattice data of every octave and
-// the corner-table offset of the lane's cell) is read once per chunk into registers, so a
-// sample-octave loads only its y and z axis data and its eight corners. The operations on
-// the values are those of dens_solid_tab, in the same order.
+// The own rows of a 32^3 density chunk from the lattice tables with lane = z: a warp takes
+// one y at a time, lane z testing the samples (x, y, z) of its row (y, z) and gathering
+// their bits in a register, so no ballot is needed. The samples of a row are taken in blocks
+// of kDensXB x coordinates, octave by octave, each keeping its fBm sum in a register (the
+// per-sample sums see the same operations in the same order as octave-inner loops would).
+// Within an octave the lattice cell along x changes rarely (every 1 / frequency voxels), so
+// the four corner-pair records the lane's samples read — columns x0 and x0 + 1 at y0 and
+// y0 + 1, each the gradients of corners z and z + 1 — stay in registers until it does, with
+// the products g.y * y and g.z * z, which do not depend on x, computed once per load. The two
+// corners of a record are evaluated together as f32x2 pairs: the eight gradient dot
+// products as four pairs, the four x lerps as two, the two y lerps as one, then the z lerp of
+// the pair's halves. Every value is the result of the operations of dens_solid_tab, in the
+// same order.
+constexpr int kDensXB = 8;
 template <int N, int LAYOUT>
-__device__ __forceinline__ void dens_rows_lane_x(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int oy) {
-  static_assert(N == 32, "lane = x needs 32-voxel rows");
+__device__ __forceinline__ void dens_rows_lane_z(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int oy) {
+  static_assert(N == 32 && N % kDensXB == 0, "lane = z needs 32-voxel rows");
+  using P = DensPlan<N>;
   const int* hdr = reinterpret_cast<const int*>(s.stage);
-  const DensAxis* axes = reinterpret_cast<const DensAxis*>(s.stage + 64);
-  const float4* corners = reinterpret_cast<const float4*>(s.stage + 64 + kDensMaxOct * 3 * (N + 2) * 16);
+  const DensAxis* axes = reinterpret_cast<const DensAxis*>(s.stage + P::kAxes);
+  const ulonglong2* pack_x = reinterpret_cast<const ulonglong2*>(s.stage + P::kPackX);
+  const ulonglong2* pack_y = reinterpret_cast<const ulonglong2*>(s.stage + P::kPackY);
+  const ulonglong2* pair_xy = reinterpret_cast<const ulonglong2*>(s.stage + P::kPairXY);
+  const f2_t* pair_z = reinterpret_cast<const f2_t*>(s.stage + P::kPairZ);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  float xf[kDensMaxOct], x1[kDensMaxOct], u[kDensMaxOct];
-  int P[kDensMaxOct], n2[kDensMaxOct], sx[kDensMaxOct];
-#pragma unroll
-  for (int o = 0; o < kDensMaxOct; ++o) {
-    xf[o] = x1[o] = u[o] = 0.0f;
-    P[o] = n2[o] = sx[o] = 0;
-    if (o < g.octaves) {
-      const DensAxis ax = axes[o * 3 * (N + 2) + lane + 1];
-      n2[o] = hdr[4 * o + 2];
-      sx[o] = hdr[4 * o + 1] * n2[o];
-      P[o] = hdr[4 * o] + ax.ci * sx[o];
-      xf[o] = ax.fr;
-      x1[o] = ax.fr1;
-      u[o] = ax.fade;
-    }
-  }
   uint32_t* occw = reinterpret_cast<uint32_t*>(s.occ);
-  for (int row = warp; row < N * N; row += nwarps) {
-    const int y = row / N, z = row % N;
-    float sum = 0.0f, amp = 1.0f;
+  for (int y = warp; y < N; y += nwarps) {
+    const float ty = ((float)(oy + y) - g.y_ref) * g.y_scale;
+    uint32_t row = 0u;
+#pragma unroll 1
+    for (int xs = 0; xs < N; xs += kDensXB) {
+      float sum[kDensXB];
 #pragma unroll
-    for (int o = 0; o < kDensMaxOct; ++o) {
-      if (o < g.octaves) {
-        const DensAxis* ao = axes + o * 3 * (N + 2);
-        const DensAxis ay = ao[(N + 2) + y + 1], az = ao[2 * (N + 2) + z + 1];
-        const float4* C = corners + P[o] + ay.ci * n2[o] + az.ci;
-        const int S = sx[o], Z = n2[o];
-        const float4 g000 = C[0], g100 = C[S], g010 = C[Z], g110 = C[S + Z];
-        const float4 g001 = C[1], g101 = C[S + 1], g011 = C[Z + 1], g111 = C[S + Z + 1];
-        const float xx = xf[o], yf = ay.fr, zf = az.fr, xm = x1[o], y1 = ay.fr1, z1 = az.fr1;
-        const float uu = u[o], v = ay.fade, w = az.fade;
-        const float l00 = d_lerp(uu, (g000.x * xx + g000.y * yf) + g000.z * zf,
-                                 (g100.x * xm + g100.y * yf) + g100.z * zf);
-        const float l10 = d_lerp(uu, (g010.x * xx + g010.y * y1) + g010.z * zf,
-                                 (g110.x * xm + g110.y * y1) + g110.z * zf);
-        const float l01 = d_lerp(uu, (g001.x * xx + g001.y * yf) + g001.z * z1,
-                                 (g101.x * xm + g101.y * yf) + g101.z * z1);
-        const float l11 = d_lerp(uu, (g011.x * xx + g011.y * y1) + g011.z * z1,
-                                 (g111.x * xm + g111.y * y1) + g111.z * z1);
-        const float n = d_lerp(w, d_lerp(v, l00, l10), d_lerp(v, l01, l11));
-        sum = sum + amp * n;
+      for (int i = 0; i < kDensXB; ++i) sum[i] = 0.0f;
+      float amp = 1.0f;
+#pragma unroll 1
+      for (int o = 0; o < g.octaves; ++o) {
+        const DensAxis az = axes[o * 3 * (N + 2) + 2 * (N + 2) + lane + 1];
+        const ulonglong2 ya = pack_y[2 * (o * (N + 2) + y + 1)];      // {yf, yf} {yf-1, yf-1}
+        const ulonglong2 yb = pack_y[2 * (o * (N + 2) + y + 1) + 1];  // {v, v} {y0, y1 offsets}
+        const f2_t zz = f2_pack(az.fr, az.fr1);
+        const int zo = hdr[4 * o] + az.ci;
+        const int ry0 = zo + (int)(unsigned)yb.y, ry1 = zo + (int)(unsigned)(yb.y >> 32);
+        const ulonglong2* px = pack_x + 2 * (o * (N + 2) + xs + 1);
+        int cur = -1;  // x offset of the records held (offsets are >= 0)
+        f2_t gx00 = 0, gx10 = 0, gx01 = 0, gx11 = 0;  // {gx} of columns (x0|x1, y0|y1)
+        f2_t py00 = 0, py10 = 0, py01 = 0, py11 = 0;  // {gy * y}
+        f2_t pz00 = 0, pz10 = 0, pz01 = 0, pz11 = 0;  // {gz * zf, gz' * (zf - 1)}
+#pragma unroll
+        for (int i = 0; i < kDensXB; ++i) {
+          const ulonglong2 xa = px[2 * i];      // {xf, xf} {xf-1, xf-1}
+          const ulonglong2 xb = px[2 * i + 1];  // {u, u} {x0, x1 offsets}
+          const int c0 = (int)(unsigned)xb.y;
+          if (c0 != cur) {  // the same in every lane
+            cur = c0;
+            const int c1 = (int)(unsigned)(xb.y >> 32);
+            const ulonglong2 q00 = pair_xy[c0 + ry0], q10 = pair_xy[c1 + ry0];
+            const ulonglong2 q01 = pair_xy[c0 + ry1], q11 = pair_xy[c1 + ry1];
+            gx00 = q00.x, gx10 = q10.x, gx01 = q01.x, gx11 = q11.x;
+            py00 = f2_mul(q00.y, ya.x), py10 = f2_mul(q10.y, ya.x);
+            py01 = f2_mul(q01.y, ya.y), py11 = f2_mul(q11.y, ya.y);
+            pz00 = f2_mul(pair_z[c0 + ry0], zz), pz10 = f2_mul(pair_z[c1 + ry0], zz);
+            pz01 = f2_mul(pair_z[c0 + ry1], zz), pz11 = f2_mul(pair_z[c1 + ry1], zz);
+          }
+          // (g.x * x + g.y * y) + g.z * z of corners (x_, y_, z) and (x_, y_, z + 1)
+          const f2_t d00 = f2_add(f2_add(f2_mul(gx00, xa.x), py00), pz00);
+          const f2_t d10 = f2_add(f2_add(f2_mul(gx10, xa.y), py10), pz10);
+          const f2_t d01 = f2_add(f2_add(f2_mul(gx01, xa.x), py01), pz01);
+          const f2_t d11 = f2_add(f2_add(f2_mul(gx11, xa.y), py11), pz11);
+          const f2_t l0 = f2_lerp(xb.x, d00, d10);  // {l00, l01}
+          const f2_t l1 = f2_lerp(xb.x, d01, d11);  // {l10, l11}
+          float m0, m1;
+          f2_unpack(f2_lerp(yb.x, l0, l1), m0, m1);
+          sum[i] = sum[i] + amp * d_lerp(az.fade, m0, m1);
+        }
         amp = amp * g.gain;
       }
+#pragma unroll
+      for (int i = 0; i < kDensXB; ++i) {
+        const float d = sum[i] - ty;
+        const bool solid = g.solid_below_zero ? (d < 0.0f) : (d > 0.0f);
+        row |= (uint32_t)solid << (xs + i);
+      }
     }
-    const int wy = oy + y;
-    const float d = sum - ((float)wy - g.y_ref) * g.y_scale;
-    const unsigned b = __ballot_sync(0xffffffffu, g.solid_below_zero ? (d < 0.0f) : (d > 0.0f));
-    if (lane == 0) occw[row] = b;
+    occw[y * N + lane] = row;
   }
 }
 
@@ -873,7 +978,7 @@ __device__ void gen_chunk(ChunkSmem<N, LAYOUT>& s, const GenDev& g, vox_chunk_co
   uint32_t* occw = reinterpret_cast<uint32_t*>(s.occ);
   const bool tab = GM == GM_DENSITY && dens_tables<N, LAYOUT, T>(s, g, ox, oy, oz);
   if (N == 32 && tab) {
-    if constexpr (N == 32) dens_rows_lane_x<N, LAYOUT>(s, g, oy);
+    if constexpr (N == 32) dens_rows_lane_z<N, LAYOUT>(s, g, oy);
   } else {
     for (int base = warp * 32; base < N * N * N; base += nwarps * 32) {
       const int e = base + lane;
@@ -2111,45 +2216,75 @@ k_mesh_single(MeshArgs a) {
 
 // Chunk::new for n chunks, occupancy rows written to global memory. One CTA per chunk:
 // chunk i at occ_out + i * words, or at slot a.slots[i] of a pool of a.pool_slots slots when
-// a.slots is set (an out-of-range slot writes nothing and latches ERR_BAD_INPUT). With LOOP:
-// chunks blockIdx.x, + gridDim.x, ... below the count *a.n_dev read from device memory (at
-// most a.n), each at occ_out + i * words; a grid of a few CTAs per SM then serves any count
-// and costs one check per CTA when there is nothing to generate.
-template <int N, int GM, int T, bool LOOP>
-__global__ void __launch_bounds__(T)
+// a.slots is set (an out-of-range slot writes nothing and latches ERR_BAD_INPUT).
+template <int N, int GM, int T>
+__global__ void __launch_bounds__(T, 65536 / (T * 64))
 k_generate(MeshArgs a, uint32_t* occ_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ChunkSmem<N, VOX_LAYOUT_VERTEX> s;
   s.carve(smem_raw);
   constexpr int words = N * N * Shape<N>::W;
-  if constexpr (LOOP) {
-    const int count = (int)min((unsigned)a.n, *a.n_dev);
-    if ((int)blockIdx.x >= count) return;  // uniform across the CTA
-    load_tables<N, VOX_LAYOUT_VERTEX>(s, a.tables);
-    __syncthreads();
-    for (int i = blockIdx.x; i < count; i += gridDim.x) {
-      gen_chunk<N, GM, VOX_LAYOUT_VERTEX, T>(s, a.gen, a.coords[i], a.index_base + i, 0u, false);
-      const uint32_t* src = reinterpret_cast<const uint32_t*>(s.occ);
-      uint32_t* dst = occ_out + (size_t)i * words;
-      for (int q = threadIdx.x; q < words; q += blockDim.x) dst[q] = src[q];
-      __syncthreads();  // the next chunk rewrites s.occ
+  const int i = blockIdx.x;
+  long long slot = i;
+  if (a.slots) {
+    slot = a.slots[i];
+    if (slot < 0 || slot >= a.pool_slots) {
+      if (threadIdx.x == 0) atomicOr(&a.ctl->err, ERR_BAD_INPUT);
+      return;  // uniform across the CTA: no barrier has been reached yet
     }
-  } else {
-    const int i = blockIdx.x;
-    long long slot = i;
-    if (a.slots) {
-      slot = a.slots[i];
-      if (slot < 0 || slot >= a.pool_slots) {
-        if (threadIdx.x == 0) atomicOr(&a.ctl->err, ERR_BAD_INPUT);
-        return;  // uniform across the CTA: no barrier has been reached yet
-      }
+  }
+  load_tables<N, VOX_LAYOUT_VERTEX>(s, a.tables);
+  __syncthreads();
+  gen_chunk<N, GM, VOX_LAYOUT_VERTEX, T>(s, a.gen, a.coords[i], a.index_base + i, 0u, false);
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(s.occ);
+  uint32_t* dst = occ_out + (size_t)slot * words;
+  for (int q = threadIdx.x; q < words; q += blockDim.x) dst[q] = src[q];
+}
+
+// The halo planes of chunks outside a batch (the staged-halo path of the fused batch):
+// for each listed chunk i below the count *a.n_dev (at most a.n), only the plane of its
+// occupancy that the meshing of its neighbour in the batch reads — x = N - 1 or x = 0 for
+// dirs[i] = 0 or 1 (the chunk is the batch chunk's -x or +x neighbour), z = N - 1 or 0 for
+// 2 or 3, y = N - 1 or 0 for 4 or 5 — written to occ_out + i * words, every other bit zero.
+// N * N samples instead of N^3; each is the sample the fused launch generates for that halo
+// plane (generation is a function of the voxel's world position). A grid of a few CTAs per
+// SM strides over the list, so the launch is sized before the count is known.
+template <int N, int GM, int T>
+__global__ void __launch_bounds__(T, 65536 / (T * 64))
+k_generate_planes(MeshArgs a, const uint8_t* __restrict__ dirs, uint32_t* occ_out) {
+  static_assert(GM == GM_HEIGHT || GM == GM_DENSITY, "planes of the noise generators only");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  ChunkSmem<N, VOX_LAYOUT_VERTEX> s;
+  s.carve(smem_raw);
+  constexpr int W = Shape<N>::W;
+  constexpr int words = N * N * W;
+  const int count = (int)min((unsigned)a.n, *a.n_dev);
+  if ((int)blockIdx.x >= count) return;  // uniform across the CTA
+  load_tables<N, VOX_LAYOUT_VERTEX>(s, a.tables);
+  uint32_t* occw = reinterpret_cast<uint32_t*>(s.occ);
+  for (int i = blockIdx.x; i < count; i += gridDim.x) {
+    for (int q = threadIdx.x; q < words; q += blockDim.x) occw[q] = 0u;
+    __syncthreads();  // (the first pass: also the tables)
+    const vox_chunk_coord c = a.coords[i];
+    const int d = dirs[i];
+    const int fix = (d & 1) ? 0 : N - 1;
+    const int ox = c.x * N, oy = c.y * N, oz = c.z * N;
+    for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
+      const int p = e / N, q = e % N;
+      const int x = d <= 1 ? fix : q;
+      const int y = d <= 3 ? p : fix;
+      const int z = d <= 1 ? q : (d <= 3 ? fix : p);
+      bool solid;
+      if constexpr (GM == GM_HEIGHT)
+        solid = y < column_k<N, VOX_LAYOUT_VERTEX>(s, a.gen, ox, oy, oz, x, z);
+      else
+        solid = gen_solid<N, GM, VOX_LAYOUT_VERTEX>(s, a.gen, x, y, z, ox, oy, oz, 0ull);
+      if (solid) atomicOr(&occw[(y * N + z) * W + (x >> 5)], 1u << (x & 31));
     }
-    load_tables<N, VOX_LAYOUT_VERTEX>(s, a.tables);
     __syncthreads();
-    gen_chunk<N, GM, VOX_LAYOUT_VERTEX, T>(s, a.gen, a.coords[i], a.index_base + i, 0u, false);
-    const uint32_t* src = reinterpret_cast<const uint32_t*>(s.occ);
-    uint32_t* dst = occ_out + (size_t)slot * words;
-    for (int q = threadIdx.x; q < words; q += blockDim.x) dst[q] = src[q];
+    uint32_t* dst = occ_out + (size_t)i * words;
+    for (int q = threadIdx.x; q < words; q += blockDim.x) dst[q] = occw[q];
+    __syncthreads();  // the next plane clears s.occ
   }
 }
 

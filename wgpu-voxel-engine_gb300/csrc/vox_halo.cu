@@ -6,8 +6,8 @@
 // path's kernel): the neighbours of chunk i are found by looking its neighbours'
 // coordinates up in a hash map of the batch (the World.chunks lookup of
 // src/chunk_builder.rs:134-169, on the device). A neighbour whose mask bit is set but that
-// is not in the batch is generated into an extra pool slot, exactly as the fused launch
-// would generate its halo.
+// is not in the batch gets an extra pool slot, into which only the plane that the meshing
+// reads is generated: the halo plane the fused launch would generate.
 #include <cstdint>
 
 #include "voxgpu.h"
@@ -78,12 +78,13 @@ __device__ __forceinline__ int map_find(const unsigned long long* keys, const in
 
 // One thread per (chunk, direction): nbr_slots[6 i + d] = the pool slot of the neighbour's
 // occupancy when mask bit d is set, else -1. A neighbour outside the batch gets an extra
-// slot n + e (its coordinate goes to extra[e]; e < extra_cap always, since every chunk and
-// direction claims at most one).
+// slot n + e (its coordinate goes to extra[e], the direction to extra_dir[e]; e < dirs * n
+// always, since every chunk and loaded direction claims at most one).
 __global__ void k_nbr_lookup(const vox_chunk_coord* __restrict__ coords,
                              const uint8_t* __restrict__ masks, int n, int dirs,
                              const unsigned long long* keys, const int* vals, unsigned cap_mask,
-                             int* nbr_slots, vox_chunk_coord* extra, unsigned* extra_count) {
+                             int* nbr_slots, vox_chunk_coord* extra, uint8_t* extra_dir,
+                             unsigned* extra_count) {
   const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (t >= 6ll * n) return;
   const int i = (int)(t / 6), d = (int)(t % 6);
@@ -97,6 +98,7 @@ __global__ void k_nbr_lookup(const vox_chunk_coord* __restrict__ coords,
     if (slot < 0) {
       const unsigned e = atomicAdd(extra_count, 1u);
       extra[e] = q;
+      extra_dir[e] = (uint8_t)d;
       slot = n + (int)e;
     }
   }
@@ -120,7 +122,7 @@ cudaError_t launch_halo_lookup(const HaloLookup& h, cudaStream_t st) {
   const long long total = 6ll * h.n;
   k_nbr_lookup<<<(unsigned)((total + T - 1) / T), T, 0, st>>>(h.coords, h.masks, h.n, h.dirs, h.keys,
                                                              h.vals, h.cap_mask, h.nbr_slots, h.extra,
-                                                             h.extra_count);
+                                                             h.extra_dir, h.extra_count);
   return cudaGetLastError();
 }
 

@@ -44,13 +44,13 @@ static KernelSet make_kernel_set() {
   k.gen_threads = Shape<N>::T1;
   k.spill_bytes = SmemPlan<N, VOX_LAYOUT_VERTEX>::kSpill;
   k.generate[0] = nullptr;
-  k.generate[GM_HEIGHT] = (const void*)k_generate<N, GM_HEIGHT, Shape<N>::T1, false>;
-  k.generate[GM_DENSITY] = (const void*)k_generate<N, GM_DENSITY, Shape<N>::T1, false>;
-  k.generate[GM_BERNOULLI] = (const void*)k_generate<N, GM_BERNOULLI, Shape<N>::T1, false>;
-  k.generate_count[0] = nullptr;
-  k.generate_count[GM_HEIGHT] = (const void*)k_generate<N, GM_HEIGHT, Shape<N>::T1, true>;
-  k.generate_count[GM_DENSITY] = (const void*)k_generate<N, GM_DENSITY, Shape<N>::T1, true>;
-  k.generate_count[GM_BERNOULLI] = (const void*)k_generate<N, GM_BERNOULLI, Shape<N>::T1, true>;
+  k.generate[GM_HEIGHT] = (const void*)k_generate<N, GM_HEIGHT, Shape<N>::T1>;
+  k.generate[GM_DENSITY] = (const void*)k_generate<N, GM_DENSITY, Shape<N>::T1>;
+  k.generate[GM_BERNOULLI] = (const void*)k_generate<N, GM_BERNOULLI, Shape<N>::T1>;
+  k.generate_planes[0] = nullptr;
+  k.generate_planes[GM_HEIGHT] = (const void*)k_generate_planes<N, GM_HEIGHT, Shape<N>::T1>;
+  k.generate_planes[GM_DENSITY] = (const void*)k_generate_planes<N, GM_DENSITY, Shape<N>::T1>;
+  k.generate_planes[GM_BERNOULLI] = nullptr;  // Bernoulli chunks have no neighbours
   k.smem_total = &smem_total_n<N>;
   return k;
 }

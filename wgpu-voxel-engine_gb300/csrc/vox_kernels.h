@@ -15,7 +15,7 @@ struct KernelSet {
   const void* overlap[4][2][2]; // k_mesh_batch_overlap<N, gen mode, layout, threads[t]>
   const void* single[2][2];     // k_mesh_single<N, layout, threads[t]>
   const void* generate[4];      // k_generate<N, gen mode, gen_threads> (index 0 unused)
-  const void* generate_count[4];// the same, the chunk count read from device memory
+  const void* generate_planes[4]; // k_generate_planes<N, gen mode, gen_threads> (height, density)
   int gen_threads;
   int spill_bytes;              // chunk state of one chunk (phased scratch)
   // dynamic shared memory of a launch (layout, CTA size, staging window in faces)
@@ -57,7 +57,8 @@ cudaError_t launch_draw_list(const Planes& planes, const void* coords,
 // coordinates (cap_mask + 1 slots, a power of two at least twice n), then per chunk and
 // direction the pool slot of the neighbour's occupancy (-1: not loaded), with the
 // neighbours that are not in the batch listed in `extra` (count in *extra_count) for slots
-// n, n + 1, ... Out-of-range coordinates latch ERR_BAD_INPUT in *err.
+// n, n + 1, ..., with the direction from the batch chunk to each in `extra_dir`.
+// Out-of-range coordinates latch ERR_BAD_INPUT in *err.
 struct HaloLookup {
   const vox_chunk_coord* coords;
   const uint8_t* masks;  // null: no neighbour is loaded
@@ -69,6 +70,7 @@ struct HaloLookup {
   int* nbr_slots;        // 6 per chunk
   int* ident;            // ident[i] = i (the batch's own pool slots)
   vox_chunk_coord* extra;
+  uint8_t* extra_dir;
   unsigned* extra_count;
   unsigned* err;
 };

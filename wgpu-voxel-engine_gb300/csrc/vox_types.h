@@ -84,8 +84,8 @@ struct MeshArgs {
   // launch of the same stream wrote as its total; every offset and output index of the
   // launch is shifted by it.
   const unsigned long long* base_ptr;
-  // k_generate: the number of chunks to generate is read from device memory (CTAs at or
-  // beyond it return at once), or null to generate all n.
+  // k_generate_planes: the number of listed chunks, read from device memory (at most n;
+  // CTAs at or beyond it return at once).
   const unsigned* n_dev;
 };
 
