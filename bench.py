@@ -63,8 +63,16 @@ NCU = {
         "traffic": 6473984, "warp_instructions": 16886488, "chunks": 1024,
         "summary": "profiles/k_mesh_batch_phased_heightmap.md"},
     ("k_mesh_batch_overlap", "density"): {
-        "traffic": 660076544, "warp_instructions": 1435145110, "chunks": 4096,
+        "traffic": 657644032, "warp_instructions": 797996508, "chunks": 4096,
         "summary": "profiles/k_mesh_batch_overlap_density.md"},
+    # staged halos: the traffic of one step's whole sequence (coordinate map, neighbour
+    # lookup, k_generate, k_generate_planes, meshing from the pool)
+    ("k_mesh_batch_overlap staged", "density"): {
+        "traffic": 650796032, "chunks": 4096, "per_step": True,
+        "summary": "profiles/staged_halo_density.md"},
+    ("k_mesh_batch_phased staged", "density"): {
+        "traffic": 688578304, "chunks": 4096, "per_step": True,
+        "summary": "profiles/staged_halo_density.md"},
     ("k_mesh_batch_overlap", "stress"): {
         "traffic": 47944924160, "chunks": 1024, "scaled_from_chunks": 48,
         "summary": "profiles/k_mesh_batch_overlap_stress.md"},
@@ -216,35 +224,60 @@ ISSUE_PEAK = 152 * 4 * 2.07e9
 # (7 each), corner gradients (2-D: 2 mul + 1 add; 3-D: 3 mul + 2 add), lerps (3 each),
 # the coordinate scaling and the fBm update (sum, amp, f).
 NOISE_OPS = {2: 2 + 2 + 14 + 2 + 4 * 3 + 3 * 3 + 2 + 4, 3: 3 + 3 + 21 + 3 + 8 * 5 + 7 * 3 + 3 + 4}
-# FP32 instruction rate with FMA contraction off (one op per instruction): 152 SMs x 128
-# lanes x 2.07 GHz. Nominal: the measured peaks file has no FP32 figure.
+# FP32 lane operations the kernels execute per sample-octave. The 2-D heightmap path
+# evaluates the whole formula per column. The 3-D lattice-table paths compute the per-axis
+# parts (floors, fractions, fades) once per coordinate: per sample they execute the corner
+# dot products, the lerps and the fBm sum (8 x 5 + 7 x 3 + 3 = 64). The 32^3 lane = z path
+# holds g.y * y and g.z * z per corner record and evaluates corner pairs as f32x2 (two lanes
+# per instruction): 4 dot pairs (1 mul + 2 adds), 2 x-lerp pairs and 1 y-lerp pair
+# (3 each) = 21 x 2, the z lerp and the sum (5), and the record products (8 pairs, at
+# least once per 8 samples: 2) = 49.
+NOISE_EXEC_OPS = {"2d": NOISE_OPS[2], "3d_table": 64, "3d_lane_z": 49}
+# FP32 lane rate: 152 SMs x 128 lanes x 2.07 GHz, one operation per lane per cycle (an f32x2
+# instruction is two). Nominal: the measured peaks file has no FP32 figure.
 FP32_OPS_NOMINAL = 152 * 128 * 2.07e9
-FP32_PEAK_SOURCE = ("nominal FP32 instruction rate (152 SMs x 128 lanes x 2.07 GHz, FMA contraction "
-                    "off); the measured-peaks file has no FP32 figure")
+FP32_PEAK_SOURCE = ("nominal FP32 lane rate (152 SMs x 128 lanes x 2.07 GHz, FMA contraction off); "
+                    "the measured-peaks file has no FP32 figure")
+
+
+def own_noise_ops(cfg):
+    """Executed FP32 lane operations per sample-octave of a chunk's own samples."""
+    if cfg.gen.kind == 0:
+        return NOISE_EXEC_OPS["2d"]
+    return NOISE_EXEC_OPS["3d_lane_z" if cfg.chunk_size == 32 else "3d_table"]
 
 
 def noise_report(wl, cfg, masks, ms_per_step):
-    """Algorithmic FP32 throughput of the noise in one step: samples x octaves x ops."""
+    """FP32 throughput of the noise in one step: samples x octaves x the lane operations
+    their path executes, against the FP32 lane rate; beside it the rate in formula operations
+    (the per-sample formula's count at the same sample rate)."""
     N = cfg.chunk_size
     g = cfg.gen
     n_chunks = len(masks)
     if g.kind == 0:    # heightmap: 2-D noise per column, (N + 2)^2 - 4 columns with halo
         samples, dim = (N + 2) ** 2 - 4, 2
         total = n_chunks * samples
+        ops = total * g.octaves * NOISE_EXEC_OPS["2d"]
     elif g.kind == 1:  # density: 3-D noise per voxel and per halo voxel of a loaded neighbour
         samples, dim = N ** 3, 3
         used = 0x3F if cfg.cull_mode == 1 else 0x0F
-        total = n_chunks * samples + sum(bin(m & used).count("1") for m in masks) * N * N
+        halo = sum(bin(m & used).count("1") for m in masks) * N * N
+        total = n_chunks * samples + halo
+        ops = (n_chunks * samples * own_noise_ops(cfg) + halo * NOISE_EXEC_OPS["3d_table"]) * g.octaves
         samples = total / n_chunks
     else:
         return None
-    ops = total * g.octaves * NOISE_OPS[dim]
     achieved = ops / (ms_per_step / 1e3)
-    return {"samples_per_chunk": samples, "octaves": g.octaves, "ops_per_sample_octave": NOISE_OPS[dim],
+    formula = total * g.octaves * NOISE_OPS[dim] / (ms_per_step / 1e3)
+    return {"samples_per_chunk": samples, "octaves": g.octaves,
+            "exec_ops_per_sample_octave": ops / (total * g.octaves),
+            "formula_ops_per_sample_octave": NOISE_OPS[dim],
             "achieved_tops": achieved / 1e12, "peak_tops": FP32_OPS_NOMINAL / 1e12,
             "peak_source": FP32_PEAK_SOURCE, "frac": achieved / FP32_OPS_NOMINAL,
-            "note": "the fused launch also culls and emits; this is the noise share of the step's "
-                    "time budget, not the noise kernel alone"}
+            "formula_tops": formula / 1e12,
+            "note": "executed lane operations of the step's noise over the whole step time (the "
+                    "launch also culls and emits); formula_tops counts the per-sample formula's "
+                    "operations at the same sample rate"}
 
 
 def cpu_baseline(wl, cfg, masks, seconds: float, threads: int = 0):
@@ -404,7 +437,7 @@ def measure_fused(name, args, torch, stream, flush, world=1, rank=0, local=0, he
     kname = {"phased": "k_mesh_batch_phased", "overlap": "k_mesh_batch_overlap"}.get(
         run.tuning.get("schedule"), "k_mesh_batch")
     staged = run.tuning.get("halo") == "pool"
-    prof = None if staged else NCU.get((kname, name))
+    prof = NCU.get((kname + (" staged" if staged else ""), name))
     if staged:  # the step is the staged-halo sequence, the meshing kernel reading the pool
         kname += " (staged halo: coordinate map, neighbour lookup, k_generate into the pool)"
     roof = {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -412,7 +445,11 @@ def measure_fused(name, args, torch, stream, flush, world=1, rank=0, local=0, he
             "algorithmic_bytes_per_step": alg_bytes, "launches_per_step": launches,
             "timing": "median CUDA-event time of one step (all its launches), L2 flushed before "
                       "each step"}
-    if prof:
+    if prof and prof.get("per_step"):
+        roof["traffic"] = prof["traffic"] * n / prof["chunks"]
+        roof["traffic_source"] = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum summed over one "
+                                  f"step's kernels ({prof['summary']}), per step like achieved")
+    elif prof:
         per_launch_chunks = n / launches
         roof["traffic"] = prof["traffic"] * per_launch_chunks / prof["chunks"]
         roof["traffic_source"] = (f"ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
@@ -537,13 +574,15 @@ def noise_kernel(ctx, wl, cfg, stream, flush, args, torch):
                              steps, stream, flush, torch)
     assert ctx.sync(raise_on_error=False) == 0
     ms = statistics.median(step_ms)
-    ops = n * samples * g.octaves * NOISE_OPS[dim]
+    ops = n * samples * g.octaves * own_noise_ops(cfg)
     achieved = ops / (ms / 1e3)
     return {"kernel": "k_generate", "ms": ms, "steps": steps, "chunks": n,
             "samples_per_chunk": samples, "octaves": g.octaves,
-            "ops_per_sample_octave": NOISE_OPS[dim], "achieved_tops": achieved / 1e12,
+            "exec_ops_per_sample_octave": own_noise_ops(cfg),
+            "formula_ops_per_sample_octave": NOISE_OPS[dim], "achieved_tops": achieved / 1e12,
             "peak_tops": FP32_OPS_NOMINAL / 1e12, "peak_source": FP32_PEAK_SOURCE,
             "frac": achieved / FP32_OPS_NOMINAL,
+            "formula_tops": n * samples * g.octaves * NOISE_OPS[dim] / (ms / 1e3) / 1e12,
             "occupancy_bytes": n * ctx.sizes.occ_words_per_chunk * 4,
             "api": "vox_generate (occupancy to a device pool, L2 flushed before each step)"}
 

@@ -1664,6 +1664,13 @@ __device__ void emit_chunk_direct(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c,
 // Kernels
 // ------------------------------------------------------------------------------------
 
+// Minimum resident CTAs per SM the fused kernels are compiled for (a register cap for the
+// 3-D density generator of 32^3 chunks, whose noise loop would otherwise take ~120).
+template <int N, int GM, int T>
+__host__ __device__ constexpr int fused_min_ctas() {
+  return (N == 32 && GM == GM_DENSITY) ? (T == 256 ? 3 : 2) : 1;
+}
+
 // Persistent fused generation + meshing over a device work queue (GM != GM_OCC), or
 // meshing of resident occupancy (GM == GM_OCC). One chunk per CTA iteration; T threads.
 // Occupancy and halo rows of chunk i in shared memory: loaded from the slot pool
@@ -1700,7 +1707,7 @@ __device__ __forceinline__ void prepare_chunk(ChunkSmem<N, LAYOUT>& s, const Mes
 }
 
 template <int N, int GM, int LAYOUT, int T>
-__global__ void __launch_bounds__(T)
+__global__ void __launch_bounds__(T, fused_min_ctas<N, GM, T>())
 k_mesh_batch(const __grid_constant__ MeshArgs a, const __grid_constant__ TablesDev tab) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ChunkSmem<N, LAYOUT> s;
@@ -1864,7 +1871,7 @@ __device__ unsigned long long scan_counts(const uint32_t* counts, int n,
 }
 
 template <int N, int GM, int LAYOUT, int T>
-__global__ void __launch_bounds__(T)
+__global__ void __launch_bounds__(T, fused_min_ctas<N, GM, T>())
 k_mesh_batch_phased(const __grid_constant__ MeshArgs a, const __grid_constant__ TablesDev tab) {
   using P = SmemPlan<N, LAYOUT>;
   // spill slot of a chunk: [occ | halo | rows] [nz] [vlist] [misc], laid out as in shared
@@ -2017,7 +2024,7 @@ k_mesh_batch_phased(const __grid_constant__ MeshArgs a, const __grid_constant__ 
 // ------------------------------------------------------------------------------------
 
 template <int N, int GM, int LAYOUT, int T>
-__global__ void __launch_bounds__(T)
+__global__ void __launch_bounds__(T, fused_min_ctas<N, GM, T>())
 k_mesh_batch_overlap(const __grid_constant__ MeshArgs a, const __grid_constant__ TablesDev tab) {
   using P = SmemPlan<N, LAYOUT>;
   constexpr int kFixed16 = (P::kOcc + P::kHalo + P::kRows) / 16;

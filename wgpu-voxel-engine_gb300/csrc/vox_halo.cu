@@ -38,12 +38,14 @@ __device__ __forceinline__ unsigned hash_key(unsigned long long k) {
   return (unsigned)k;
 }
 
-// Inserts coords[i] -> i (the first insert of a coordinate keeps its index).
+// Inserts coords[i] -> i (the first insert of a coordinate keeps its index) and writes the
+// identity slot ident[i] = i (the batch's own pool slots).
 __global__ void k_map_insert(const vox_chunk_coord* __restrict__ coords, int n,
-                             unsigned long long* keys, int* vals, unsigned cap_mask,
+                             unsigned long long* keys, int* vals, unsigned cap_mask, int* ident,
                              unsigned* err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
+  ident[i] = i;
   unsigned long long key;
   if (!coord_key(coords[i], key)) {
     atomicOr(err, ERR_BAD_INPUT);
@@ -105,11 +107,6 @@ __global__ void k_nbr_lookup(const vox_chunk_coord* __restrict__ coords,
   nbr_slots[t] = slot;
 }
 
-__global__ void k_identity(int* out, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) out[i] = i;
-}
-
 }  // namespace
 
 cudaError_t launch_halo_lookup(const HaloLookup& h, cudaStream_t st) {
@@ -117,8 +114,8 @@ cudaError_t launch_halo_lookup(const HaloLookup& h, cudaStream_t st) {
   if (e != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(h.extra_count, 0, sizeof(unsigned), st)) != cudaSuccess) return e;
   const int T = 256;
-  k_map_insert<<<(h.n + T - 1) / T, T, 0, st>>>(h.coords, h.n, h.keys, h.vals, h.cap_mask, h.err);
-  k_identity<<<(h.n + T - 1) / T, T, 0, st>>>(h.ident, h.n);
+  k_map_insert<<<(h.n + T - 1) / T, T, 0, st>>>(h.coords, h.n, h.keys, h.vals, h.cap_mask, h.ident,
+                                                h.err);
   const long long total = 6ll * h.n;
   k_nbr_lookup<<<(unsigned)((total + T - 1) / T), T, 0, st>>>(h.coords, h.masks, h.n, h.dirs, h.keys,
                                                              h.vals, h.cap_mask, h.nbr_slots, h.extra,

@@ -54,9 +54,9 @@ class BatchRun:
         slab = t.slab_chunks if 0 < t.slab_chunks < n else n
         self.launches_per_step = (n + slab - 1) // slab
         if t.halo_staging:
-            # staged halos: coordinate map, identity slots, neighbour lookup, generation of
-            # the batch and (with neighbour masks) of the neighbours outside it
-            self.launches_per_step += 4 + (1 if masks is not None else 0)
+            # staged halos: coordinate map (with the identity slots), neighbour lookup,
+            # generation of the batch and (with neighbour masks) of the halo planes outside it
+            self.launches_per_step += 3 + (1 if masks is not None else 0)
         self.graph = (ctx.capture_graph(self.d_coords, self.d_mask, n, self.out0, self.out1,
                                         self.cap, self.offsets, chunk_index_base=index_base)
                       if graph else None)
