@@ -1664,11 +1664,22 @@ __device__ void emit_chunk_direct(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c,
 // Kernels
 // ------------------------------------------------------------------------------------
 
-// Minimum resident CTAs per SM the fused kernels are compiled for (a register cap for the
-// 3-D density generator of 32^3 chunks, whose noise loop would otherwise take ~120).
+// Minimum resident CTAs per SM the fused kernels are compiled for, i.e. their register
+// budget: 64 registers a thread in general (4 CTAs of 256 threads), which keeps the
+// meshing paths at the occupancy their shared memory allows. The 3-D density generator
+// needs more: 80 at 256 threads for 32^3 chunks (3 CTAs), 64 at 512 (2 CTAs); 16^3 and 8^3
+// chunks keep the budgets the compiler chose for them unconstrained, and 64^3 density or
+// heightmap chunks at 512 threads keep up to 128.
 template <int N, int GM, int T>
 __host__ __device__ constexpr int fused_min_ctas() {
-  return (N == 32 && GM == GM_DENSITY) ? (T == 256 ? 3 : 2) : 1;
+  if (GM == GM_DENSITY) {
+    if (N == 32) return T == 256 ? 3 : 2;
+    if (N == 16) return T == 256 ? 3 : 7;
+    if (N == 8) return T == 64 ? 14 : 25;
+    return 1;
+  }
+  if (GM == GM_HEIGHT && N == 64 && T == 512) return 1;
+  return 65536 / (T * 64) > 0 ? 65536 / (T * 64) : 1;
 }
 
 // Persistent fused generation + meshing over a device work queue (GM != GM_OCC), or
@@ -2221,11 +2232,21 @@ k_mesh_single(MeshArgs a) {
   if ((threadIdx.x & 31) == 0) bulk_wait_all();
 }
 
+// Register budget of k_generate as resident CTAs per SM: 64 registers a thread for the 3-D
+// density noise (its lane = z loop holds a block of sums and four corner records), 32 for
+// the heightmap columns up to 32^3 and for Bernoulli fills, whose occupancy then follows
+// shared memory alone.
+template <int N, int GM, int T>
+__host__ __device__ constexpr int generate_min_ctas() {
+  if (GM == GM_DENSITY || (GM == GM_HEIGHT && N > 32)) return 65536 / (T * 64) > 0 ? 65536 / (T * 64) : 1;
+  return 65536 / (T * 32) > 32 ? 32 : 65536 / (T * 32);
+}
+
 // Chunk::new for n chunks, occupancy rows written to global memory. One CTA per chunk:
 // chunk i at occ_out + i * words, or at slot a.slots[i] of a pool of a.pool_slots slots when
 // a.slots is set (an out-of-range slot writes nothing and latches ERR_BAD_INPUT).
 template <int N, int GM, int T>
-__global__ void __launch_bounds__(T, 65536 / (T * 64))
+__global__ void __launch_bounds__(T, generate_min_ctas<N, GM, T>())
 k_generate(MeshArgs a, uint32_t* occ_out) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   ChunkSmem<N, VOX_LAYOUT_VERTEX> s;
