@@ -34,6 +34,15 @@ def gen_cfg(vox, kind, n, layout=0, cull=0):
         return vox.make_config(chunk_size=n, layout=layout, cull_mode=cull, kind=vox.GEN_DENSITY,
                                octaves=3, seed=1234, frequency=1 / 96, y_ref=float(n // 2),
                                y_scale=1 / 64)
+    if kind == "density4":  # the most octaves the lattice-table path takes
+        return vox.make_config(chunk_size=n, layout=layout, cull_mode=cull, kind=vox.GEN_DENSITY,
+                               octaves=4, seed=4321, frequency=1 / 64, y_ref=float(n // 2),
+                               y_scale=1 / 48)
+    if kind == "density1x":  # one octave, lattice cells 5 voxels wide (corner records reloaded
+        # several times per block of x samples on the 32^3 path)
+        return vox.make_config(chunk_size=n, layout=layout, cull_mode=cull, kind=vox.GEN_DENSITY,
+                               octaves=1, seed=9, frequency=0.2, y_ref=float(n // 2),
+                               y_scale=1 / 24)
     if kind == "density6":  # more octaves than the lattice-table path takes (per-sample path)
         return vox.make_config(chunk_size=n, layout=layout, cull_mode=cull, kind=vox.GEN_DENSITY,
                                octaves=6, seed=77, frequency=1 / 40, y_ref=float(n // 2),
@@ -51,8 +60,8 @@ def gen_cfg(vox, kind, n, layout=0, cull=0):
 
 
 @pytest.mark.parametrize("n", [8, 16, 32, 64])
-@pytest.mark.parametrize("kind", ["height", "height1", "density", "density6", "densityhf",
-                                  "refdensity", "bernoulli"])
+@pytest.mark.parametrize("kind", ["height", "height1", "density", "density4", "density1x",
+                                  "density6", "densityhf", "refdensity", "bernoulli"])
 def test_generate_matches_oracle(vox, oracle, n, kind):
     cfg = gen_cfg(vox, kind, n)
     coords = small_coords()
@@ -702,4 +711,35 @@ def test_randomized_batches_match_oracle(vox, oracle, case):
     assert np.array_equal(to_np(o0, total * b0), w0), tag
     if b1:
         assert np.array_equal(to_np(o1, total * b1), w1), tag
+    ctx.close()
+
+
+@pytest.mark.parametrize("n", [16, 32])
+@pytest.mark.parametrize("kind", ["density4", "density1x", "refdensity"])
+@pytest.mark.parametrize("halo", [0, 1])
+def test_density_configs_fused_and_staged(vox, oracle, n, kind, halo):
+    """Density generators at the table path's limits (4 octaves; lattice cells narrower
+    than a block of x samples) through the fused launch (halos regenerated: per-sample
+    table reads) and the staged-halo path (generation kernel, then meshing from the pool)."""
+    rng = np.random.default_rng(77 + n + 3 * halo)
+    cull = int(rng.integers(0, 2))
+    cfg = gen_cfg(vox, kind, n, cull=cull)
+    m = 20
+    coords = [tuple(int(v) for v in rng.integers(-4, 4, 3)) for _ in range(m)]
+    coords = list(dict.fromkeys(coords))  # distinct, so every chunk has one pool slot
+    m = len(coords)
+    masks = [int(v) for v in rng.integers(0, 64 if cull else 16, m)]
+    w0, w1, woffs = oracle.gen_mesh_batch(cfg, coords, masks, 0)
+    total = int(woffs[-1])
+    ctx = ctx_for(vox, cfg)
+    t = ctx.tuning()
+    ctx.set_tuning(t.threads, t.stage_faces, 0, 2, 0, halo)
+    o0, o1 = dev_bytes(max(total, 1) * 96), dev_bytes(max(total, 1) * 24)
+    offs = to_dev(np.zeros(m + 1, np.uint64))
+    ctx.gen_mesh_batch(to_dev(np.asarray(coords, np.int32)), to_dev(np.asarray(masks, np.uint8)), m,
+                       o0, o1, total, offs)
+    ctx.sync()
+    assert np.array_equal(to_np(offs), woffs), (n, kind, halo)
+    assert np.array_equal(to_np(o0, total * 96), w0), (n, kind, halo)
+    assert np.array_equal(to_np(o1, total * 24), w1), (n, kind, halo)
     ctx.close()
