@@ -63,7 +63,7 @@ NCU = {
         "traffic": 6473984, "warp_instructions": 16886488, "chunks": 1024,
         "summary": "profiles/k_mesh_batch_phased_heightmap.md"},
     ("k_mesh_batch_overlap", "density"): {
-        "traffic": 657644032, "warp_instructions": 797996508, "chunks": 4096,
+        "traffic": 658092032, "warp_instructions": 707898692, "chunks": 4096,
         "summary": "profiles/k_mesh_batch_overlap_density.md"},
     # staged halos: the traffic of one step's whole sequence (coordinate map, neighbour
     # lookup, k_generate, k_generate_planes, meshing from the pool)

@@ -962,6 +962,84 @@ __device__ __forceinline__ void dens_rows_lane_z(ChunkSmem<N, LAYOUT>& s, const 
   }
 }
 
+// One lateral halo plane of a 32^3 density chunk (h = 0..3: x = -1, x = N, z = -1, z = N)
+// from the lattice tables, evaluated like the own rows: lane b is the sample's z (x planes)
+// or x (z planes), a warp takes a contiguous run of RB rows y, octave by octave, with the
+// run's sums in registers, and the four corner-pair records stay in registers while the y
+// lattice cell is unchanged, with g.x * x and g.z * z computed once per load. Row y of the
+// plane is the ballot over the lanes. Every value is the result of the operations of
+// dens_solid_tab, in the same order.
+template <int N, int LAYOUT, int RB>
+__device__ __forceinline__ void dens_halo_plane_pairs(ChunkSmem<N, LAYOUT>& s, const GenDev& g, int oy,
+                                                      int h) {
+  static_assert(N == 32, "one sample per lane along the plane");
+  using P = DensPlan<N>;
+  const int* hdr = reinterpret_cast<const int*>(s.stage);
+  const DensAxis* axes = reinterpret_cast<const DensAxis*>(s.stage + P::kAxes);
+  const ulonglong2* pack_x = reinterpret_cast<const ulonglong2*>(s.stage + P::kPackX);
+  const ulonglong2* pack_y = reinterpret_cast<const ulonglong2*>(s.stage + P::kPackY);
+  const ulonglong2* pair_xy = reinterpret_cast<const ulonglong2*>(s.stage + P::kPairXY);
+  const f2_t* pair_z = reinterpret_cast<const f2_t*>(s.stage + P::kPairZ);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int y0 = warp * RB;
+  const int fixed = (h & 1) ? N + 1 : 0;  // table index of -1 or N
+  const int xi = h < 2 ? fixed : lane + 1, zi = h < 2 ? lane + 1 : fixed;
+  float sum[RB];
+#pragma unroll
+  for (int i = 0; i < RB; ++i) sum[i] = 0.0f;
+  float amp = 1.0f;
+#pragma unroll 1
+  for (int o = 0; o < g.octaves; ++o) {
+    const ulonglong2 xa = pack_x[2 * (o * (N + 2) + xi)];      // {xf, xf} {xf-1, xf-1}
+    const ulonglong2 xb = pack_x[2 * (o * (N + 2) + xi) + 1];  // {u, u} {x0, x1 offsets}
+    const DensAxis az = axes[o * 3 * (N + 2) + 2 * (N + 2) + zi];
+    const f2_t zz = f2_pack(az.fr, az.fr1);
+    const int zo = hdr[4 * o] + az.ci;
+    const int c0 = zo + (int)(unsigned)xb.y, c1 = zo + (int)(unsigned)(xb.y >> 32);
+    int cur = -1;  // y offset of the records held (offsets are >= 0)
+    f2_t gy00 = 0, gy10 = 0, gy01 = 0, gy11 = 0;  // {gy} of columns (x0|x1, y0|y1)
+    f2_t px00 = 0, px10 = 0, px01 = 0, px11 = 0;  // {gx * x}
+    f2_t pz00 = 0, pz10 = 0, pz01 = 0, pz11 = 0;  // {gz * zf, gz' * (zf - 1)}
+#pragma unroll
+    for (int i = 0; i < RB; ++i) {
+      const int y = y0 + i;
+      const ulonglong2 ya = pack_y[2 * (o * (N + 2) + y + 1)];      // {yf, yf} {yf-1, yf-1}
+      const ulonglong2 yb = pack_y[2 * (o * (N + 2) + y + 1) + 1];  // {v, v} {y0, y1 offsets}
+      const int r0 = (int)(unsigned)yb.y;
+      if (r0 != cur) {  // the same in every lane
+        cur = r0;
+        const int r1 = (int)(unsigned)(yb.y >> 32);
+        const ulonglong2 q00 = pair_xy[c0 + r0], q10 = pair_xy[c1 + r0];
+        const ulonglong2 q01 = pair_xy[c0 + r1], q11 = pair_xy[c1 + r1];
+        gy00 = q00.y, gy10 = q10.y, gy01 = q01.y, gy11 = q11.y;
+        px00 = f2_mul(q00.x, xa.x), px10 = f2_mul(q10.x, xa.y);
+        px01 = f2_mul(q01.x, xa.x), px11 = f2_mul(q11.x, xa.y);
+        pz00 = f2_mul(pair_z[c0 + r0], zz), pz10 = f2_mul(pair_z[c1 + r0], zz);
+        pz01 = f2_mul(pair_z[c0 + r1], zz), pz11 = f2_mul(pair_z[c1 + r1], zz);
+      }
+      // (g.x * x + g.y * y) + g.z * z of corners (x_, y_, z) and (x_, y_, z + 1)
+      const f2_t d00 = f2_add(f2_add(px00, f2_mul(gy00, ya.x)), pz00);
+      const f2_t d10 = f2_add(f2_add(px10, f2_mul(gy10, ya.x)), pz10);
+      const f2_t d01 = f2_add(f2_add(px01, f2_mul(gy01, ya.y)), pz01);
+      const f2_t d11 = f2_add(f2_add(px11, f2_mul(gy11, ya.y)), pz11);
+      const f2_t l0 = f2_lerp(xb.x, d00, d10);  // {l00, l01}
+      const f2_t l1 = f2_lerp(xb.x, d01, d11);  // {l10, l11}
+      float m0, m1;
+      f2_unpack(f2_lerp(yb.x, l0, l1), m0, m1);
+      sum[i] = sum[i] + amp * d_lerp(az.fade, m0, m1);
+    }
+    amp = amp * g.gain;
+  }
+  uint32_t* halow = reinterpret_cast<uint32_t*>(s.halo);
+#pragma unroll
+  for (int i = 0; i < RB; ++i) {
+    const int y = y0 + i;
+    const float d = sum[i] - ((float)(oy + y) - g.y_ref) * g.y_scale;
+    const unsigned b = __ballot_sync(0xffffffffu, g.solid_below_zero ? (d < 0.0f) : (d > 0.0f));
+    if (lane == 0) halow[h * N + y] = b;
+  }
+}
+
 // Fills s.occ (own rows) and, for every set bit of `halo_mask`, the halo rows; the other
 // halo rows are zero (a neighbour that is not loaded counts as air, chunk.rs:102-107).
 template <int N, int GM, int LAYOUT, int T>
@@ -992,6 +1070,12 @@ __device__ void gen_chunk(ChunkSmem<N, LAYOUT>& s, const GenDev& g, vox_chunk_co
     uint32_t* halow = reinterpret_cast<uint32_t*>(s.halo);
     for (int h = 0; h < 6; ++h) {
       if ((halo_mask >> h) & 1u) {
+        if constexpr (N == 32 && T >= 128) {  // N * 32 / T rows per warp
+          if (tab && h < 4) {  // lateral planes of the table path: corner pairs
+            dens_halo_plane_pairs<N, LAYOUT, N * 32 / T>(s, g, oy, h);
+            continue;
+          }
+        }
         for (int base = warp * 32; base < N * N; base += nwarps * 32) {
           const int e = base + lane;
           int x, y, z;
