@@ -3,8 +3,9 @@
 Every chunk of the batch is generated once into an occupancy pool, and for every loaded
 neighbour outside it the one plane that the meshing reads; the neighbours are found by a
 device hash lookup of the batch's coordinates, and the chunks are meshed from the pool with
-each halo plane read from the neighbour's occupancy. The bytes must be those of the fused launch, which regenerates the
-halos, and of the oracle, which generates every neighbour from its coordinate.
+each halo plane read from the neighbour's occupancy. The bytes must be those of the fused
+launch, which regenerates the halos, and of the oracle, which generates every neighbour
+from its coordinate.
 """
 import numpy as np
 import pytest
