@@ -93,6 +93,10 @@ struct Entry {
 
 enum BatchKind { kLoad = 0, kRebuild = 1 };
 
+// Pinned input bytes a slot holds per chunk: coordinates (12), occupancy slot (4),
+// neighbour slots (24), neighbour mask (1), rounded up.
+constexpr size_t kInputBytesPerChunk = 48;
+
 struct Slot {
   vox_ctx* ctx = nullptr;
   cudaStream_t stream = nullptr;
@@ -108,6 +112,10 @@ struct Slot {
   int32_t* d_nbr_slots = nullptr;  // ... and per chunk and direction (-1: absent)
   uint64_t* d_offsets = nullptr;
   uint64_t* h_offsets = nullptr;  // pinned
+  // pinned copies of the batch's inputs (coordinates, masks, occupancy and neighbour slots):
+  // the host-to-device copies run asynchronously from them; the slot reuses them only after
+  // its batch has finished
+  unsigned char* h_inputs = nullptr;
   std::vector<vox_chunk_coord> chunks;
   std::vector<int32_t> occ_slots;  // host copies of d_slots
   std::vector<uint8_t> nbr_used;   // per chunk: the neighbours its mesh is built with
@@ -316,13 +324,20 @@ int launch_batch(vox_serve* s, Slot& sl, int kind, std::vector<vox_chunk_coord>&
   sl.seq = ++s->launch_seq;
   sl.launched_at = mono_now();
   cudaEventRecord(sl.start, sl.stream);
-  cudaMemcpyAsync(sl.d_coords, chunks.data(), sizeof(vox_chunk_coord) * m, cudaMemcpyHostToDevice,
+  // pinned inputs: [coords | occupancy slots | neighbour slots | masks], each 4-byte aligned
+  const size_t mcap = (size_t)s->cfg.max_batch;
+  vox_chunk_coord* h_coords = reinterpret_cast<vox_chunk_coord*>(sl.h_inputs);
+  int32_t* h_slots = reinterpret_cast<int32_t*>(sl.h_inputs + 12 * mcap);
+  int32_t* h_nbr = reinterpret_cast<int32_t*>(sl.h_inputs + 16 * mcap);
+  uint8_t* h_mask = sl.h_inputs + 40 * mcap;
+  std::memcpy(h_coords, chunks.data(), sizeof(vox_chunk_coord) * m);
+  cudaMemcpyAsync(sl.d_coords, h_coords, sizeof(vox_chunk_coord) * m, cudaMemcpyHostToDevice,
                   sl.stream);
   int st;
   std::vector<uint8_t> used(m, 0);
   if (!rb) {
-    std::vector<uint8_t> masks(m, s->cfg.chunk.cull_mode == VOX_CULL_FULL6 ? 0x3F : 0x0F);
-    cudaMemcpyAsync(sl.d_mask, masks.data(), (size_t)m, cudaMemcpyHostToDevice, sl.stream);
+    std::memset(h_mask, s->cfg.chunk.cull_mode == VOX_CULL_FULL6 ? 0x3F : 0x0F, (size_t)m);
+    cudaMemcpyAsync(sl.d_mask, h_mask, (size_t)m, cudaMemcpyHostToDevice, sl.stream);
     st = vox_gen_mesh_batch(sl.ctx, sl.d_coords, sl.d_mask, m, 0, blk->out0, blk->out1, cap,
                             sl.d_offsets);
   } else {
@@ -341,8 +356,10 @@ int launch_batch(vox_serve* s, Slot& sl, int kind, std::vector<vox_chunk_coord>&
         nbr[(size_t)6 * i + d] = slot;
         if (slot >= 0) used[i] |= (uint8_t)(1u << d);
       }
-    cudaMemcpyAsync(sl.d_slots, occ.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, sl.stream);
-    cudaMemcpyAsync(sl.d_nbr_slots, nbr.data(), sizeof(int32_t) * 6 * m, cudaMemcpyHostToDevice,
+    std::memcpy(h_slots, occ.data(), sizeof(int32_t) * m);
+    std::memcpy(h_nbr, nbr.data(), sizeof(int32_t) * 6 * m);
+    cudaMemcpyAsync(sl.d_slots, h_slots, sizeof(int32_t) * m, cudaMemcpyHostToDevice, sl.stream);
+    cudaMemcpyAsync(sl.d_nbr_slots, h_nbr, sizeof(int32_t) * 6 * m, cudaMemcpyHostToDevice,
                     sl.stream);
     st = kind == kLoad ? vox_generate_slots(sl.ctx, sl.d_coords, m, 0, s->d_occ_pool,
                                             s->occ_pool_slots, sl.d_slots)
@@ -506,10 +523,16 @@ bool any_busy(const vox_serve* s) {
   return false;
 }
 
+// wait: block until the oldest batch in flight has finished (the other slots keep running
+// while it is integrated and refilled).
 int poll_and_admit(vox_serve* s, bool wait) {
+  const Slot* oldest = nullptr;
+  if (wait)
+    for (const Slot& sl : s->slots)
+      if (sl.busy && (!oldest || sl.seq < oldest->seq)) oldest = &sl;
   for (Slot& sl : s->slots) {
     if (!sl.busy) continue;
-    cudaError_t q = wait ? cudaEventSynchronize(sl.done) : cudaEventQuery(sl.done);
+    cudaError_t q = &sl == oldest ? cudaEventSynchronize(sl.done) : cudaEventQuery(sl.done);
     if (q == cudaErrorNotReady) continue;
     if (q != cudaSuccess) return VOX_ERR_CUDA;
     // Completion time from the GPU's own timestamps (the slot's stream is idle when a
@@ -527,11 +550,15 @@ int poll_and_admit(vox_serve* s, bool wait) {
   const size_t fit = (size_t)std::max<uint64_t>(1, s->cfg.cache_budget_bytes / per_chunk);
   const size_t batch = std::min<size_t>((size_t)s->cfg.max_batch, fit);
   if (!s->queue.empty()) {
-    if (!s->queue_sorted)
-      std::stable_sort(s->queue.begin(), s->queue.end(),
-                       [s](const vox_chunk_coord& a, const vox_chunk_coord& b) {
-                         return dist2(s, a) < dist2(s, b);
-                       });
+    if (!s->queue_sorted) {
+      // stable by distance: (distance, position) keys, every distance computed once
+      std::vector<std::pair<float, uint32_t>> key(s->queue.size());
+      for (size_t i = 0; i < key.size(); ++i) key[i] = {dist2(s, s->queue[i]), (uint32_t)i};
+      std::sort(key.begin(), key.end());
+      std::vector<vox_chunk_coord> sorted(key.size());
+      for (size_t i = 0; i < key.size(); ++i) sorted[i] = s->queue[key[i].second];
+      s->queue.swap(sorted);
+    }
     s->queue_sorted = true;
     size_t head = 0;
     for (Slot& sl : s->slots) {
@@ -643,7 +670,8 @@ int vox_serve_create(const vox_serve_config* cfg, vox_serve** out) {
         cudaMalloc(&sl.d_slots, sizeof(int32_t) * cfg->max_batch) != cudaSuccess ||
         cudaMalloc(&sl.d_nbr_slots, sizeof(int32_t) * 6 * cfg->max_batch) != cudaSuccess ||
         cudaMalloc(&sl.d_offsets, sizeof(uint64_t) * (cfg->max_batch + 1)) != cudaSuccess ||
-        cudaMallocHost(&sl.h_offsets, sizeof(uint64_t) * (cfg->max_batch + 1)) != cudaSuccess)
+        cudaMallocHost(&sl.h_offsets, sizeof(uint64_t) * (cfg->max_batch + 1)) != cudaSuccess ||
+        cudaMallocHost(&sl.h_inputs, kInputBytesPerChunk * (size_t)cfg->max_batch) != cudaSuccess)
       return VOX_ERR_OOM;
   }
   if (cfg->neighbour_rebuild) {
@@ -681,6 +709,7 @@ int vox_serve_destroy(vox_serve* s) {
     cudaFree(sl.d_nbr_slots);
     cudaFree(sl.d_offsets);
     if (sl.h_offsets) cudaFreeHost(sl.h_offsets);
+    if (sl.h_inputs) cudaFreeHost(sl.h_inputs);
     if (sl.done) cudaEventDestroy(sl.done);
     if (sl.start) cudaEventDestroy(sl.start);
     if (sl.stream) cudaStreamDestroy(sl.stream);
@@ -728,6 +757,10 @@ int vox_serve_submit(vox_serve* s, const vox_chunk_coord* coords, int32_t n, dou
   vox::TraceRange trace_("vox_serve_submit");
   if (!s || n < 0 || (n > 0 && !coords)) return VOX_ERR_INVALID;
   if (now_s < 0.0) now_s = mono_now();
+  // room for every new request at once (no rehash per growth step)
+  s->entries.reserve(s->entries.size() + (size_t)n);
+  s->by_id.reserve(s->by_id.size() + (size_t)n);
+  s->queue.reserve(s->queue.size() + (size_t)n);
   for (int32_t i = 0; i < n; ++i) {
     const uint64_t id = request(s, coords[i], now_s);
     if (ids_out) ids_out[i] = id;

@@ -481,7 +481,7 @@ class Server:
         st = self._lib.vox_serve_submit(self._h, c.ctypes.data, len(c), now, ids.ctypes.data)
         if st != VOX_OK:
             raise VoxError(st, "vox_serve_submit")
-        return [int(v) for v in ids]
+        return ids.tolist()
 
     def poll(self, req_id) -> int:
         """VOX_REQ_UNKNOWN, VOX_REQ_PENDING or VOX_REQ_RESIDENT."""
