@@ -282,6 +282,35 @@ float dist2(const vox_serve* s, const vox_chunk_coord& c) {
   return dx * dx + dy * dy + dz * dz;
 }
 
+// Orders q by distance from the eye, ties in their current order (a stable sort): a
+// least-significant-digit radix sort on the bits of the squared distances, every distance
+// computed once (a non-negative float's bit pattern orders like the float).
+void sort_by_distance(const vox_serve* s, std::vector<vox_chunk_coord>& q) {
+  const size_t n = q.size();
+  std::vector<uint32_t> key(n), key2(n);
+  std::vector<uint32_t> idx(n), idx2(n);
+  for (size_t i = 0; i < n; ++i) {
+    const float d = dist2(s, q[i]);
+    std::memcpy(&key[i], &d, sizeof d);
+    idx[i] = (uint32_t)i;
+  }
+  for (int shift = 0; shift < 32; shift += 8) {
+    size_t count[257] = {0};
+    for (size_t i = 0; i < n; ++i) ++count[((key[i] >> shift) & 255u) + 1];
+    for (int b = 0; b < 256; ++b) count[b + 1] += count[b];
+    for (size_t i = 0; i < n; ++i) {
+      const size_t at = count[(key[i] >> shift) & 255u]++;
+      key2[at] = key[i];
+      idx2[at] = idx[i];
+    }
+    key.swap(key2);
+    idx.swap(idx2);
+  }
+  std::vector<vox_chunk_coord> sorted(n);
+  for (size_t i = 0; i < n; ++i) sorted[i] = q[idx[i]];
+  q.swap(sorted);
+}
+
 Entry* resident_entry(vox_serve* s, const vox_chunk_coord& c) {
   auto it = s->entries.find(c);
   return it != s->entries.end() && it->second.state == Entry::RESIDENT ? &it->second : nullptr;
@@ -650,15 +679,7 @@ int poll_and_admit(vox_serve* s, bool wait) {
   const size_t fit = (size_t)std::max<uint64_t>(1, s->cfg.cache_budget_bytes / per_chunk);
   const size_t batch = std::min<size_t>((size_t)s->cfg.max_batch, fit);
   if (!s->queue.empty()) {
-    if (!s->queue_sorted) {
-      // stable by distance: (distance, position) keys, every distance computed once
-      std::vector<std::pair<float, uint32_t>> key(s->queue.size());
-      for (size_t i = 0; i < key.size(); ++i) key[i] = {dist2(s, s->queue[i]), (uint32_t)i};
-      std::sort(key.begin(), key.end());
-      std::vector<vox_chunk_coord> sorted(key.size());
-      for (size_t i = 0; i < key.size(); ++i) sorted[i] = s->queue[key[i].second];
-      s->queue.swap(sorted);
-    }
+    if (!s->queue_sorted) sort_by_distance(s, s->queue);
     s->queue_sorted = true;
     size_t head = 0;
     for (Slot& sl : s->slots) {
