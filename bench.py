@@ -584,6 +584,11 @@ def noise_kernel(ctx, wl, cfg, stream, flush, args, torch):
             "frac": achieved / FP32_OPS_NOMINAL,
             "formula_tops": n * samples * g.octaves * NOISE_OPS[dim] / (ms / 1e3) / 1e12,
             "occupancy_bytes": n * ctx.sizes.occ_words_per_chunk * 4,
+            "bound": ("FP32 pipe (FMA pipe 64 % active under ncu, math_pipe_throttle the top stall: "
+                      "profiles/k_generate_density.md)" if g.kind == 1 else
+                      "latency: one wave of one-chunk CTAs, each evaluating its columns' fBm as "
+                      "chains of dependent permutation-table reads and writing 1 KiB; the FP32 "
+                      "fraction is not this kernel's bound"),
             "api": "vox_generate (occupancy to a device pool, L2 flushed before each step)"}
 
 
