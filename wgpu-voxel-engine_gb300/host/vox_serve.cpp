@@ -772,7 +772,7 @@ int vox_serve_create(const vox_serve_config* cfg, vox_serve** out) {
   s->dirs = cfg->chunk.cull_mode == VOX_CULL_FULL6 ? 6 : 4;
   s->bytes_per_face = s->sizes.bytes_per_face_out0 + s->sizes.bytes_per_face_out1;
   s->est_faces_per_chunk = (uint64_t)4 * s->n * s->n;
-  // keep freed blocks in the stream-ordered pool instead of returning them to the driver
+  // keep freed blocks in the stream-ordered pool instead of returning them to the CUDA driver
   int dev = 0;
   cudaGetDevice(&dev);
   cudaMemPool_t pool;
