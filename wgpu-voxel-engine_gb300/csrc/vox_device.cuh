@@ -1570,6 +1570,11 @@ __device__ __forceinline__ int emit_elems(const ChunkSmem<N, LAYOUT>& s) {
 // bulk copy that last read a buffer is done before refilling it, and until all its
 // copies have read shared memory at the end (the staging area is reused by the next
 // chunk's generation).
+// Faces per whole number of 128-byte output lines: 16 for the 96-byte vertex and 24-byte
+// index records, 32 for the 68-byte instance records.
+template <int LAYOUT>
+__host__ __device__ constexpr unsigned line_faces() { return LAYOUT == VOX_LAYOUT_INSTANCED ? 32u : 16u; }
+
 // Sends the nwf faces of a warp's face list (chunk-local indices first, first + 1, ...) to
 // global faces g0 + first + ...: 32 at a time staged in one of the warp's nbuf buffers
 // (`bufs`, buffer index b carried across calls) and sent by a TMA bulk copy, or by
@@ -1583,9 +1588,12 @@ __device__ __forceinline__ void warp_send_faces(const TablesDev* tab, const uint
   constexpr int kBuf = warp_buf_bytes<LAYOUT>();
   const int ox = c.x * N, oy = c.y * N, oz = c.z * N;
   const int lane = threadIdx.x & 31;
-  for (int r0 = 0; r0 < nwf; r0 += kWarpBatch) {
-    const int cnt = nwf - r0 < kWarpBatch ? nwf - r0 : kWarpBatch;
+  for (int r0 = 0, cnt = 0; r0 < nwf; r0 += cnt) {
     const unsigned long long g = g0 + first + (unsigned)r0;
+    // a batch that starts off a line_faces boundary of the output ends on a later one, so
+    // that the batches after it cover whole 128-byte lines
+    cnt = kWarpBatch - (int)(g & (unsigned long long)(line_faces<LAYOUT>() - 1u));
+    if (cnt > nwf - r0) cnt = nwf - r0;
     int nw = cnt;
     if (g >= cap) nw = 0;
     else if (g + (unsigned long long)cnt > cap) nw = (int)(cap - g);
@@ -1619,10 +1627,16 @@ __device__ __forceinline__ void warp_send_faces(const TablesDev* tab, const uint
 
 // Emission of elements [lo, hi): warp w takes the contiguous run [lo + w*per, ...) of
 // whole groups of 32 elements, so consecutive groups' faces are adjacent in the output.
-// Faces accumulate in the warp's list and leave in full batches of 32 (the send step);
-// fewer than 32 are carried to the next group, and the rest leave at the end.
+// Faces accumulate in the warp's list and leave once there are at least 32, up to the last
+// line_faces boundary of the output (g0: the output index of chunk-local face 0); fewer
+// than line_faces are carried to the next group, and the rest leave at the end. Batches
+// that start and end on those boundaries write whole 128-byte lines, which matters most
+// for outputs in host memory, where a partial line costs a slower write.
 template <int N, int LAYOUT, typename Send>
-__device__ __forceinline__ void emit_runs(ChunkSmem<N, LAYOUT>& s, int lo, int hi, Send send) {
+__device__ __forceinline__ void emit_runs(ChunkSmem<N, LAYOUT>& s, int lo, int hi,
+                                          unsigned long long g0, Send send) {
+  constexpr unsigned kLine = line_faces<LAYOUT>();
+  const unsigned phase = (unsigned)(g0 & (unsigned long long)(kLine - 1u));
   const bool use_list = s.misc[1] >= 0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   uint32_t* list = s.lists + warp * kWarpFaces;
@@ -1637,7 +1651,7 @@ __device__ __forceinline__ void emit_runs(ChunkSmem<N, LAYOUT>& s, int lo, int h
     const int nwf = warp_faces<N, LAYOUT>(s, use_list, whi, base, list + have, first);
     if (have == 0) first_have = first;
     have += nwf;
-    const int full = have & ~31;
+    const int full = have >= 32 ? have - (int)((phase + first_have + (unsigned)have) & (kLine - 1u)) : 0;
     if (full > 0) {
       send(list, full, first_have);
       // move the remainder (< 32 faces) to the front of the list
@@ -1664,7 +1678,7 @@ __device__ void emit_chunk(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c, unsigned 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned char* bufs = s.stage + (size_t)warp * nbuf * kBuf;
   int b = 0;
-  emit_runs<N, LAYOUT>(s, lo, hi, [&](const uint32_t* list, int nf, uint32_t first) {
+  emit_runs<N, LAYOUT>(s, lo, hi, g0, [&](const uint32_t* list, int nf, uint32_t first) {
     warp_send_faces<N, LAYOUT>(s.tab, list, nf, first, c, g0, cap, out0, out1, bufs, nbuf,
                                lane_flush, b);
   });
@@ -1739,7 +1753,7 @@ template <int N, int LAYOUT>
 __device__ void emit_chunk_direct(ChunkSmem<N, LAYOUT>& s, vox_chunk_coord c,
                                   unsigned long long g0, unsigned long long cap, void* out0,
                                   void* out1, int lo, int hi) {
-  emit_runs<N, LAYOUT>(s, lo, hi, [&](const uint32_t* list, int nf, uint32_t first) {
+  emit_runs<N, LAYOUT>(s, lo, hi, g0, [&](const uint32_t* list, int nf, uint32_t first) {
     warp_store_faces<N, LAYOUT>(s.tab, list, nf, first, c, g0, cap, out0, out1);
   });
 }
