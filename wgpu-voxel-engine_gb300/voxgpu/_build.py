@@ -74,6 +74,8 @@ def build_library(verbose: bool = False, extra_nvcc=None) -> str:
     os.makedirs(BUILD_DIR, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
+    if os.path.isdir(HOST):
+        headers += [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith(".h")]
     hdr_time = _newest(headers)
     cu = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
     cpp = sorted(f for f in os.listdir(CSRC) if f.endswith(".cpp"))
