@@ -33,6 +33,7 @@
 #include "voxgpu.h"
 #include "voxgpu_serve.h"
 #include "vox_flat_map.h"
+#include "vox_order.h"
 #include "../csrc/vox_trace.h"
 
 namespace {
@@ -176,32 +177,16 @@ float dist2(const vox_serve* s, const vox_chunk_coord& c) {
   return dx * dx + dy * dy + dz * dz;
 }
 
-// Orders q by distance from the eye, ties in their current order (a stable sort): a
-// least-significant-digit radix sort on the bits of the squared distances, every distance
-// computed once (a non-negative float's bit pattern orders like the float).
+// Orders q by distance from the eye, ties in their current order (a stable sort), every
+// distance computed once.
 void sort_by_distance(const vox_serve* s, std::vector<vox_chunk_coord>& q) {
   const size_t n = q.size();
-  std::vector<uint32_t> key(n), key2(n);
-  std::vector<uint32_t> idx(n), idx2(n);
-  for (size_t i = 0; i < n; ++i) {
-    const float d = dist2(s, q[i]);
-    std::memcpy(&key[i], &d, sizeof d);
-    idx[i] = (uint32_t)i;
-  }
-  for (int shift = 0; shift < 32; shift += 8) {
-    size_t count[257] = {0};
-    for (size_t i = 0; i < n; ++i) ++count[((key[i] >> shift) & 255u) + 1];
-    for (int b = 0; b < 256; ++b) count[b + 1] += count[b];
-    for (size_t i = 0; i < n; ++i) {
-      const size_t at = count[(key[i] >> shift) & 255u]++;
-      key2[at] = key[i];
-      idx2[at] = idx[i];
-    }
-    key.swap(key2);
-    idx.swap(idx2);
-  }
+  std::vector<float> d(n);
+  for (size_t i = 0; i < n; ++i) d[i] = dist2(s, q[i]);
+  std::vector<uint32_t> order;
+  vox::radix_order(d.data(), n, order);
   std::vector<vox_chunk_coord> sorted(n);
-  for (size_t i = 0; i < n; ++i) sorted[i] = q[idx[i]];
+  for (size_t i = 0; i < n; ++i) sorted[i] = q[order[i]];
   q.swap(sorted);
 }
 
