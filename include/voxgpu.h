@@ -252,11 +252,12 @@ typedef struct vox_tuning {
                           the output right after the previous one's (same bytes and offsets
                           as one launch); 0 = the whole batch in one launch */
   int32_t halo_staging;/* 0: each chunk's lateral halo is regenerated in shared memory by the
-                          fused launch; 1: every chunk of the batch (and every loaded
-                          neighbour outside it) is generated once into an occupancy pool, and
-                          the chunks are meshed from the pool with each halo plane read from
-                          the neighbour's occupancy, the neighbours being found by a hash
-                          lookup of the batch's coordinates. Same bytes either way; mode 1
+                          fused launch; 1: every chunk of the batch is generated once into an
+                          occupancy pool (and, for every loaded neighbour outside the batch,
+                          the one plane its batch neighbour reads), and the chunks are meshed
+                          from the pool with each halo plane read from the neighbour's
+                          occupancy, the neighbours being found by a hash lookup of the
+                          batch's coordinates. Same bytes either way; mode 1
                           needs chunk coordinates within [-2^20, 2^20) (otherwise
                           VOX_ERR_INVALID from vox_ctx_sync) and applies to outputs in device
                           memory: vox_gen_mesh_host with page-locked outputs keeps mode 0,
