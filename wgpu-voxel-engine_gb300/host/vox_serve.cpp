@@ -376,7 +376,16 @@ int launch_batch(vox_serve* s, Slot& sl, int kind, std::vector<vox_chunk_coord>&
       st = vox_mesh_batch(sl.ctx, s->d_occ_pool, s->occ_pool_slots, sl.d_slots, sl.d_nbr_slots,
                           sl.d_coords, m, blk->out0, blk->out1, cap, sl.d_offsets);
   }
-  if (st != VOX_OK) return st;
+  if (st != VOX_OK) {
+    // nothing of the batch is kept: the block is freed behind whatever the stream already
+    // runs, and the occupancy slots taken above return once that work has finished
+    cudaStreamSynchronize(sl.stream);
+    s->stats.cache_bytes -= bytes;
+    free_block(blk.get());
+    if (need_occ)
+      for (int32_t o : occ) s->occ_free.push_back(o);
+    return st;
+  }
   cudaMemcpyAsync(sl.h_offsets, sl.d_offsets, sizeof(uint64_t) * (m + 1), cudaMemcpyDeviceToHost,
                   sl.stream);
   cudaEventRecord(sl.done, sl.stream);
@@ -567,7 +576,10 @@ int poll_and_admit(vox_serve* s, bool wait) {
       std::vector<vox_chunk_coord> chunks(s->queue.begin() + head, s->queue.begin() + head + take);
       const int st = launch_batch(s, sl, kLoad, std::move(chunks), {});
       if (st == VOX_ERR_OOM) break;  // the cache is full of visible chunks: retry later
-      if (st != VOX_OK) return st;
+      if (st != VOX_OK) {
+        s->queue.erase(s->queue.begin(), s->queue.begin() + head);  // those are on the GPU
+        return st;
+      }
       head += take;
     }
     s->queue.erase(s->queue.begin(), s->queue.begin() + head);
@@ -617,6 +629,10 @@ int rebuild_candidates(vox_serve* s, vox_chunk_coord c) {
     cudaFree(s->d_cand);
     cudaFree(s->d_vis);
     cudaFreeHost(s->h_vis);
+    s->d_cand = nullptr;
+    s->d_vis = nullptr;
+    s->h_vis = nullptr;
+    s->cand_cap = 0;
     if (cudaMalloc(&s->d_cand, n * sizeof(vox_chunk_coord)) != cudaSuccess ||
         cudaMalloc(&s->d_vis, n) != cudaSuccess || cudaMallocHost(&s->h_vis, n) != cudaSuccess)
       return VOX_ERR_OOM;
