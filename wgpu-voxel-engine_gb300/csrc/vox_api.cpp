@@ -66,7 +66,7 @@ struct vox_ctx {
   GenDev gen{};
   int gm = GM_HEIGHT;
   // tuning: CTA-size option, staging window (0 = direct stores), resident CTAs per SM,
-  // schedule (look-back or phased)
+  // schedule (look-back, phased or overlap)
   int topt = 0;
   int stage_faces = 0;
   int ctas_per_sm = 0;
@@ -79,7 +79,7 @@ struct vox_ctx {
   int phased_grid[4] = {0, 0, 0, 0};  // co-resident grid per gen mode (phased kernel)
   int overlap_grid[4] = {0, 0, 0, 0}; // persistent grid per gen mode (overlap kernel)
   int host_grid[4] = {0, 0, 0, 0};    // grid of launches that write host memory (staged)
-  // phased schedule: per-chunk occupancy + halo spill and face totals
+  // phased and overlap schedules: per-chunk occupancy + halo spill and face totals
   uint32_t* d_scratch = nullptr;
   uint32_t* d_counts = nullptr;
   size_t scratch_cap = 0;  // chunks
@@ -451,10 +451,11 @@ int ensure_halo(vox_ctx* ctx, HaloScratch& h, size_t n) {
 
 // The staged-halo pre-pass of a fused batch `a` (generator mode gm): the neighbour lookup,
 // then every chunk of the batch generated into the pool, and for every loaded neighbour
-// outside it the one plane its batch neighbour reads; `a` becomes the equivalent batch over resident occupancy (GM_OCC). The bytes it
-// then writes are the fused launch's: a halo plane read from the neighbour's occupancy is
-// the plane the fused launch generates (generation is a function of the voxel's world
-// position; Bernoulli chunks have no neighbours).
+// outside it the one plane its batch neighbour reads; `a` becomes the equivalent batch over
+// resident occupancy (GM_OCC). The bytes it then writes are the fused launch's: a halo
+// plane read from the neighbour's occupancy is the plane the fused launch generates
+// (generation is a function of the voxel's world position; Bernoulli chunks have no
+// neighbours).
 int halo_prepass(vox_ctx* ctx, MeshArgs& a, int gm, HaloScratch& h, cudaStream_t stream) {
   const size_t words = (size_t)ctx->ks->n_size * ctx->ks->n_size *
                        (ctx->ks->n_size > 32 ? ctx->ks->n_size / 32 : 1);
@@ -701,7 +702,9 @@ static int sync_locked(vox_ctx* ctx) {
            "cudaMemcpyAsync(ctl)");
   VOX_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "cudaStreamSynchronize");
   if (err & ERR_TIMEOUT) return fail(ctx, VOX_ERR_TIMEOUT, "a device-side wait gave up");
-  if (err & ERR_BAD_INPUT) return fail(ctx, VOX_ERR_INVALID, "a slot index was out of range");
+  if (err & ERR_BAD_INPUT)
+    return fail(ctx, VOX_ERR_INVALID,
+                "a slot index, or (staged halos) a chunk coordinate, was out of range");
   return fail(ctx, VOX_ERR_CAPACITY, "output capacity exceeded");
 }
 

@@ -10,7 +10,7 @@ namespace vox {
 
 constexpr unsigned ERR_TIMEOUT = 1u;   // a look-back wait gave up
 constexpr unsigned ERR_CAPACITY = 2u;  // output capacity exceeded
-constexpr unsigned ERR_BAD_INPUT = 4u; // a slot index out of range
+constexpr unsigned ERR_BAD_INPUT = 4u; // a slot index, or a hashed coordinate, out of range
 // set in a status mirror word by the launch that wrote it (MeshArgs::err_mirror)
 constexpr unsigned kMirrorValid = 0x80000000u;
 
