@@ -21,9 +21,12 @@ from . import _build
 __all__ = [
     "VOX_OK", "VOX_ERR_INVALID", "VOX_ERR_OOM", "VOX_ERR_CUDA", "VOX_ERR_TIMEOUT",
     "VOX_ERR_CAPACITY", "VOX_ERR_NO_DEVICE", "GEN_HEIGHTMAP", "GEN_DENSITY", "GEN_BERNOULLI",
-    "CULL_REFERENCE", "CULL_FULL6", "LAYOUT_VERTEX", "LAYOUT_INSTANCED", "ChunkCoord",
-    "Generator", "Config", "Sizes", "VoxError", "lib", "Context", "GRASS_TEXTURES",
-    "frustum_planes", "neighbour_masks", "grid_coords",
+    "CULL_REFERENCE", "CULL_FULL6", "LAYOUT_VERTEX", "LAYOUT_INSTANCED", "SCHEDULE_LOOKBACK",
+    "SCHEDULE_PHASED", "SCHEDULE_OVERLAP", "VOX_REQ_UNKNOWN", "VOX_REQ_PENDING",
+    "VOX_REQ_RESIDENT", "GRASS_TEXTURES", "ChunkCoord", "Generator", "Config", "Sizes",
+    "Tuning", "ServeConfig", "ServeStats", "VoxError", "lib", "make_config", "query_sizes",
+    "frustum_planes", "Context", "Graph", "camera_matrix", "Server", "serving_camera",
+    "grid_coords", "neighbour_masks", "Workload", "workload",
 ]
 
 VOX_OK, VOX_ERR_INVALID, VOX_ERR_OOM, VOX_ERR_CUDA = 0, 1, 2, 3
@@ -43,6 +46,8 @@ class ChunkCoord(ctypes.Structure):
 
 
 class Generator(ctypes.Structure):
+    """vox_generator: the terrain generator (heightmap, density or Bernoulli) and its
+    noise parameters."""
     _fields_ = [
         ("kind", ctypes.c_int32), ("octaves", ctypes.c_int32), ("seed", ctypes.c_uint64),
         ("frequency", ctypes.c_float), ("lacunarity", ctypes.c_float), ("gain", ctypes.c_float),
@@ -52,6 +57,7 @@ class Generator(ctypes.Structure):
 
 
 class Config(ctypes.Structure):
+    """vox_config: chunk size, cull mode, output layout, texture slots and generator."""
     _fields_ = [
         ("chunk_size", ctypes.c_int32), ("cull_mode", ctypes.c_int32), ("layout", ctypes.c_int32),
         ("texture_index", ctypes.c_uint32 * 6), ("gen", Generator),
@@ -59,6 +65,8 @@ class Config(ctypes.Structure):
 
 
 class Sizes(ctypes.Structure):
+    """vox_sizes: occupancy words per chunk, bytes per face of each output, faces per chunk
+    at most."""
     _fields_ = [
         ("occ_words_per_chunk", ctypes.c_uint32), ("bytes_per_face_out0", ctypes.c_uint32),
         ("bytes_per_face_out1", ctypes.c_uint32), ("max_faces_per_chunk", ctypes.c_uint32),
@@ -66,11 +74,13 @@ class Sizes(ctypes.Structure):
 
 
 class Tuning(ctypes.Structure):
+    """vox_tuning: launch shape, schedule, output slab and halo staging of a context."""
     _fields_ = [("threads", ctypes.c_int32), ("stage_faces", ctypes.c_int32),
                 ("ctas_per_sm", ctypes.c_int32), ("schedule", ctypes.c_int32),
                 ("slab_chunks", ctypes.c_int32), ("halo_staging", ctypes.c_int32)]
 
     def as_dict(self):
+        """The tuning with the schedule and the halo staging by name."""
         return {"threads": self.threads, "stage_faces": self.stage_faces,
                 "ctas_per_sm": self.ctas_per_sm,
                 "schedule": {SCHEDULE_PHASED: "phased", SCHEDULE_OVERLAP: "overlap"}.get(
@@ -80,6 +90,8 @@ class Tuning(ctypes.Structure):
 
 
 class ServeConfig(ctypes.Structure):
+    """vox_serve_config: the streaming engine's chunk config, view disk, batching and cache
+    budget."""
     _fields_ = [("chunk", Config), ("view_radius", ctypes.c_int32), ("y_min", ctypes.c_int32),
                 ("y_max", ctypes.c_int32), ("max_batch", ctypes.c_int32),
                 ("slots", ctypes.c_int32), ("cache_budget_bytes", ctypes.c_uint64),
@@ -87,6 +99,7 @@ class ServeConfig(ctypes.Structure):
 
 
 class ServeStats(ctypes.Structure):
+    """vox_serve_stats: the streaming engine's counters and request-to-mesh latency."""
     _fields_ = [("frames", ctypes.c_uint64), ("requested", ctypes.c_uint64),
                 ("completed", ctypes.c_uint64), ("evicted", ctypes.c_uint64),
                 ("launches", ctypes.c_uint64), ("faces_resident", ctypes.c_uint64),
@@ -97,10 +110,14 @@ class ServeStats(ctypes.Structure):
                 ("rebuilt", ctypes.c_uint64), ("rebuild_launches", ctypes.c_uint64)]
 
     def as_dict(self):
+        """Every field by name."""
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class VoxError(RuntimeError):
+    """A non-zero status of a C ABI call (where the reference would panic), with the
+    context's last error message."""
+
     def __init__(self, status: int, what: str, detail: str = ""):
         self.status = status
         msg = f"{what}: status {status}"
@@ -213,6 +230,7 @@ def make_config(chunk_size=32, cull_mode=CULL_REFERENCE, layout=LAYOUT_VERTEX, k
                 octaves=1, seed=42, frequency=1.0 / 64, lacunarity=2.0, gain=0.5, amplitude=12.0,
                 base_height=4.0, y_ref=0.0, y_scale=0.0, solid_below_zero=0,
                 textures=GRASS_TEXTURES) -> Config:
+    """A vox_config from keyword arguments (the generator's fields flattened)."""
     cfg = Config()
     cfg.chunk_size = chunk_size
     cfg.cull_mode = cull_mode
@@ -228,6 +246,7 @@ def make_config(chunk_size=32, cull_mode=CULL_REFERENCE, layout=LAYOUT_VERTEX, k
 
 
 def query_sizes(cfg: Config) -> Sizes:
+    """vox_query_sizes: the buffer sizes a config needs."""
     s = Sizes()
     st = lib().vox_query_sizes(ctypes.byref(cfg), ctypes.byref(s))
     if st != VOX_OK:
@@ -260,6 +279,7 @@ class Context:
         self._graphs = weakref.WeakSet()
 
     def close(self):
+        """vox_ctx_destroy, after the context's captured graphs."""
         if getattr(self, "_h", None):
             for g in list(getattr(self, "_graphs", ())):
                 g.close()  # a graph needs its context
@@ -283,6 +303,7 @@ class Context:
 
     @property
     def stream(self) -> int:
+        """The context's CUDA stream (vox_ctx_stream)."""
         return int(self._lib.vox_ctx_stream(self._h) or 0)
 
     def _check(self, st: int, what: str):
@@ -291,32 +312,37 @@ class Context:
             raise VoxError(st, what, detail)
 
     def sync(self, raise_on_error: bool = True) -> int:
+        """vox_ctx_sync: waits for the context's work and returns its latched status."""
         st = self._lib.vox_ctx_sync(self._h)
         if raise_on_error:
             self._check(st, "vox_ctx_sync")
         return st
 
-    # Chunk::new
     def generate(self, d_coords, n: int, d_occ, chunk_index_base: int = 0):
+        """vox_generate (Chunk::new, src/chunk.rs:21-46): occupancy of n chunks."""
         self._check(self._lib.vox_generate(self._h, _ptr(d_coords), n, chunk_index_base,
                                            _ptr(d_occ)), "vox_generate")
 
     def generate_slots(self, d_coords, n: int, d_pool, pool_slots: int, d_slots,
                        chunk_index_base: int = 0):
+        """vox_generate_slots: occupancy of n chunks into the given slots of a pool."""
         self._check(self._lib.vox_generate_slots(self._h, _ptr(d_coords), n, chunk_index_base,
                                                  _ptr(d_pool), pool_slots, _ptr(d_slots)),
                     "vox_generate_slots")
 
     def occ_to_cubes(self, d_occ, n: int, d_cubes):
+        """vox_occ_to_cubes: occupancy to the reference's one byte per voxel (Vec<Cube>)."""
         self._check(self._lib.vox_occ_to_cubes(self._h, _ptr(d_occ), n, _ptr(d_cubes)),
                     "vox_occ_to_cubes")
 
     def cubes_to_occ(self, d_cubes, n: int, d_occ):
+        """vox_cubes_to_occ: one byte per voxel back to occupancy."""
         self._check(self._lib.vox_cubes_to_occ(self._h, _ptr(d_cubes), n, _ptr(d_occ)),
                     "vox_cubes_to_occ")
 
-    # Chunk::create_mesh
     def mesh(self, d_occ, nbrs, coord, d_out0, d_out1, cap_faces: int, d_count):
+        """vox_mesh (Chunk::create_mesh, src/chunk.rs:48-245): one chunk with explicit
+        neighbour occupancy (None: absent)."""
         arr = (_P * 6)(*[_P(_ptr(b)) for b in (list(nbrs) + [None] * 6)[:6]])
         c = ChunkCoord(*coord)
         self._check(self._lib.vox_mesh(self._h, _ptr(d_occ), arr, c, _ptr(d_out0), _ptr(d_out1),
@@ -324,6 +350,8 @@ class Context:
 
     def mesh_batch(self, d_pool, pool_slots: int, d_slots, d_nbr_slots, d_coords, n: int, d_out0,
                    d_out1, cap_faces: int, d_offsets):
+        """vox_mesh_batch: a batch meshed from occupancy resident in a pool (the rebuild
+        path)."""
         self._check(self._lib.vox_mesh_batch(self._h, _ptr(d_pool), pool_slots, _ptr(d_slots),
                                              _ptr(d_nbr_slots), _ptr(d_coords), n, _ptr(d_out0),
                                              _ptr(d_out1), cap_faces, _ptr(d_offsets)),
@@ -331,6 +359,8 @@ class Context:
 
     def gen_mesh_batch(self, d_coords, d_nbr_mask, n: int, d_out0, d_out1, cap_faces: int,
                        d_offsets, chunk_index_base: int = 0):
+        """vox_gen_mesh_batch: generation and meshing of a batch in the fused launch
+        (Chunk::new + create_mesh per chunk, src/chunk_builder.rs:80-84), device buffers."""
         self._check(self._lib.vox_gen_mesh_batch(self._h, _ptr(d_coords), _ptr(d_nbr_mask), n,
                                                  chunk_index_base, _ptr(d_out0), _ptr(d_out1),
                                                  cap_faces, _ptr(d_offsets)),
@@ -338,6 +368,8 @@ class Context:
 
     def gen_mesh_host(self, h_coords, h_nbr_mask, n: int, h_out0, h_out1, cap_faces: int,
                       h_offsets, chunk_index_base: int = 0, raise_on_error: bool = True) -> int:
+        """vox_gen_mesh_host: as gen_mesh_batch with host buffers (page-locked outputs are
+        written in place); returns the status."""
         st = self._lib.vox_gen_mesh_host(self._h, _ptr(h_coords), _ptr(h_nbr_mask), n,
                                          chunk_index_base, _ptr(h_out0), _ptr(h_out1), cap_faces,
                                          _ptr(h_offsets))
@@ -346,17 +378,20 @@ class Context:
         return st
 
     def tuning(self) -> Tuning:
+        """vox_ctx_get_tuning."""
         t = Tuning()
         self._check(self._lib.vox_ctx_get_tuning(self._h, ctypes.byref(t)), "vox_ctx_get_tuning")
         return t
 
     def set_tuning(self, threads: int, stage_faces: int, ctas_per_sm: int = 0,
                    schedule: int = 0, slab_chunks: int = 0, halo_staging: int = 0):
+        """vox_ctx_set_tuning."""
         t = Tuning(threads, stage_faces, ctas_per_sm, schedule, slab_chunks, halo_staging)
         self._check(self._lib.vox_ctx_set_tuning(self._h, ctypes.byref(t)), "vox_ctx_set_tuning")
 
     def autotune(self, d_coords, d_nbr_mask, n: int, d_out0, d_out1, cap_faces: int, d_offsets,
                  chunk_index_base: int = 0, iters: int = 3) -> Tuning:
+        """vox_autotune: times the candidate tunings on this batch and keeps the fastest."""
         t = Tuning()
         self._check(self._lib.vox_autotune(self._h, _ptr(d_coords), _ptr(d_nbr_mask), n,
                                            chunk_index_base, _ptr(d_out0), _ptr(d_out1),
@@ -365,6 +400,8 @@ class Context:
         return t
 
     def selftest_lookback_timeout(self, spin_limit: int) -> int:
+        """vox_selftest_lookback_timeout: a bounded device wait made to run out; returns the
+        status (VOX_ERR_TIMEOUT)."""
         return self._lib.vox_selftest_lookback_timeout(self._h, spin_limit)
 
     def draw_list(self, planes, d_coords, d_offsets, n: int, d_draws, d_count):
@@ -387,6 +424,7 @@ class Context:
         return g
 
     def frustum_cull(self, planes, d_coords, n: int, d_visible):
+        """vox_frustum_cull (Frustum::contains, src/frustum_culling.rs:16-40) per chunk."""
         p = (ctypes.c_float * 24)(*[float(v) for v in planes])
         self._check(self._lib.vox_frustum_cull(self._h, ctypes.addressof(p), _ptr(d_coords), n,
                                                _ptr(d_visible)), "vox_frustum_cull")
@@ -400,9 +438,11 @@ class Graph:
         self._h = handle
 
     def launch(self):
+        """vox_graph_launch: one replay on the context's stream."""
         self._ctx._check(self._ctx._lib.vox_graph_launch(self._h), "vox_graph_launch")
 
     def close(self):
+        """vox_graph_destroy."""
         if self._h:
             self._ctx._lib.vox_graph_destroy(self._h)
             self._h = None
@@ -444,6 +484,7 @@ class Server:
         self._h = h
 
     def close(self):
+        """vox_serve_destroy."""
         if getattr(self, "_h", None):
             self._lib.vox_serve_destroy(self._h)
             self._h = None
@@ -459,9 +500,12 @@ class Server:
 
     @staticmethod
     def now() -> float:
+        """The engine clock (vox_serve_now), in seconds."""
         return lib().vox_serve_now()
 
     def frame(self, view_proj, eye, now=-1.0):
+        """vox_serve_frame: one camera frame (ChunkGenerator::build_chunks + World::update):
+        cull the view disk, request the visible chunks, admit batches."""
         m = (ctypes.c_float * 16)(*[float(v) for v in view_proj])
         e = (ctypes.c_float * 3)(*[float(v) for v in eye])
         st = self._lib.vox_serve_frame(self._h, ctypes.addressof(m), ctypes.addressof(e), now)
@@ -469,6 +513,7 @@ class Server:
             raise VoxError(st, "vox_serve_frame")
 
     def drain(self):
+        """vox_serve_drain: waits until every request and rebuild is resident."""
         st = self._lib.vox_serve_drain(self._h)
         if st != VOX_OK:
             raise VoxError(st, "vox_serve_drain")
@@ -500,6 +545,7 @@ class Server:
         return self._lib.vox_serve_cancel(self._h, req_id)
 
     def stats(self) -> ServeStats:
+        """vox_serve_get_stats: counters and p50/p99/max latency over every request."""
         s = ServeStats()
         st = self._lib.vox_serve_get_stats(self._h, ctypes.byref(s))
         if st != VOX_OK:
@@ -570,12 +616,14 @@ class Workload:
     isolated: bool = False
 
     def config(self, layout=LAYOUT_VERTEX, cull_mode=CULL_REFERENCE) -> Config:
+        """The workload's vox_config with the given layout and cull mode."""
         kw = dict(self.cfg_kwargs)
         kw.setdefault("layout", layout)
         kw.setdefault("cull_mode", cull_mode)
         return make_config(**kw)
 
     def masks(self, full6: bool = False):
+        """Loaded-neighbour masks of the workload's chunks (all 0 for isolated chunks)."""
         if self.isolated:
             return [0] * len(self.coords)
         return neighbour_masks(self.coords, full6)
