@@ -83,6 +83,7 @@ NCU = {
 
 
 def parse_args(argv=None):
+    """The bench's command line (the driver's --gpus/--steps/--warmup, and sub-run knobs)."""
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=400)
@@ -120,6 +121,7 @@ def parse_args(argv=None):
 
 
 def dist_info():
+    """(rank, world size, local rank) from the torchrun environment (0, 1, 0 alone)."""
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -208,6 +210,7 @@ class ClockSampler:
 
 
 def load_peak():
+    """The measured HBM copy rate (GB/s) and its source, else the fallback figure."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
         with open(path) as f:
@@ -310,6 +313,8 @@ def cpu_baseline(wl, cfg, masks, seconds: float, threads: int = 0):
 
 
 def run_reference(args):
+    """--impl reference: the reference's CPU chunk builder (the C restatement) on all host
+    threads, on rank 0 only, for the same workload, metric and config as our arm."""
     rank, world, _ = dist_info()
     if rank != 0:
         return 0
@@ -781,6 +786,8 @@ def sub_workload(name, args, torch, stream, flush, e2e_chunks=None, cpu_seconds=
 
 
 def run_ours(args):
+    """Our arm: the workload's batch on this rank's GPU (graph replays, L2 flushed), with
+    e2e, roofline, CPU baseline and, by default, the stress, density and serving sub-runs."""
     import torch
 
     rank, world, local = dist_info()
@@ -860,6 +867,7 @@ def run_ours(args):
 
 
 def run_serving(args):
+    """--workload serving: the streaming engine alone (paced frames and capacity)."""
     rank, world, local = dist_info()
     import torch
     torch.cuda.set_device(local)
@@ -879,6 +887,7 @@ def run_serving(args):
 
 
 def main():
+    """Dispatches to the reference arm, the serving run or our arm."""
     args = parse_args()
     if args.impl == "reference":
         return run_reference(args)

@@ -23,6 +23,7 @@ class _Coord(ctypes.Structure):
 
 
 def load() -> ctypes.CDLL:
+    """Loads liboracle_vox.so (built on first use) and declares its functions."""
     global _LIB
     if _LIB is not None:
         return _LIB
@@ -88,16 +89,20 @@ def _cfg_addr(cfg) -> int:
 
 
 def coords_array(coords) -> np.ndarray:
+    """Chunk coordinates as a contiguous (n, 3) int32 array."""
     return np.ascontiguousarray(np.asarray(coords, dtype=np.int32).reshape(-1, 3))
 
 
 def perm(seed: int) -> np.ndarray:
+    """The doubled noise permutation (512 bytes): Fisher-Yates over splitmix64(seed)."""
     p = np.zeros(512, np.uint8)
     load().or_perm_init(seed, _addr(p))
     return p
 
 
 def generate_cubes(cfg, coord, chunk_index: int = 0) -> np.ndarray:
+    """Chunk::new / generate_terrain (src/chunk.rs:21-46): the chunk's cubes, one byte per
+    voxel at x + N z + N^2 y (GRASS 0, AIR 2)."""
     n = cfg.chunk_size
     out = np.zeros(n * n * n, np.uint8)
     st = load().or_generate_cubes(_cfg_addr(cfg), _Coord(*coord), chunk_index, _addr(out))
@@ -106,6 +111,7 @@ def generate_cubes(cfg, coord, chunk_index: int = 0) -> np.ndarray:
 
 
 def cubes_to_occ(n: int, cubes: np.ndarray) -> np.ndarray:
+    """Cubes to occupancy rows (bit x of row y * N + z; a voxel is solid iff not AIR)."""
     w = n // 32 if n > 32 else 1
     occ = np.zeros(n * n * w, np.uint32)
     load().or_cubes_to_occ(n, _addr(np.ascontiguousarray(cubes, np.uint8)), _addr(occ))
@@ -113,6 +119,7 @@ def cubes_to_occ(n: int, cubes: np.ndarray) -> np.ndarray:
 
 
 def occ_to_cubes(n: int, occ: np.ndarray) -> np.ndarray:
+    """Occupancy rows back to cubes."""
     cubes = np.zeros(n * n * n, np.uint8)
     load().or_occ_to_cubes(n, _addr(np.ascontiguousarray(occ, np.uint32)), _addr(cubes))
     return cubes
@@ -138,12 +145,14 @@ def cull_faces(n: int, cull_mode: int, cubes: np.ndarray, adj=None) -> np.ndarra
 
 
 def face_rotation(d: int) -> np.ndarray:
+    """The 3x3 f32 rotation of face direction d (src/quad.rs:14-54: Rz * Ry * Rx)."""
     r = np.zeros((3, 3), np.float32)
     load().or_face_rotation(d, _addr(r))
     return r
 
 
 def bytes_per_face(layout: int):
+    """(out0, out1) bytes per face: instanced (68, 0), vertex/index (96, 24)."""
     return (68, 0) if layout == 1 else (96, 24)
 
 
@@ -184,6 +193,8 @@ def gen_mesh_batch(cfg, coords, masks=None, index_base: int = 0, cap: int | None
 
 
 def baseline_run(cfg, coords, masks, index_base: int, nthreads: int) -> int:
+    """The reference's pool work on the CPU: Chunk::new then create_mesh for every chunk,
+    one chunk per task on nthreads threads (src/chunk_builder.rs:80-84); returns the faces."""
     c = coords_array(coords)
     m = None if masks is None else np.ascontiguousarray(np.asarray(masks, np.uint8))
     return int(load().or_baseline_run(_cfg_addr(cfg), _addr(c), _addr(m), len(c), index_base,
@@ -240,6 +251,7 @@ def camera_global_matrix(eye, direction, aspect, fovy, znear, zfar) -> np.ndarra
 
 
 def frustum_planes(m_colmajor) -> np.ndarray:
+    """Frustum::matrix_to_planes (src/frustum_culling.rs:47-85): six planes (a, b, c, d)."""
     m = np.ascontiguousarray(np.asarray(m_colmajor, np.float32).reshape(16))
     out = np.zeros(24, np.float32)
     load().or_frustum_planes(_addr(m), _addr(out))
@@ -247,6 +259,7 @@ def frustum_planes(m_colmajor) -> np.ndarray:
 
 
 def frustum_contains(planes, coord, extent: int) -> bool:
+    """Frustum::contains (src/frustum_culling.rs:16-40) for the chunk at coord."""
     p = np.ascontiguousarray(np.asarray(planes, np.float32).reshape(24))
     return bool(load().or_frustum_contains(_addr(p), _Coord(*coord), extent))
 
@@ -263,6 +276,8 @@ def raster(view_proj, vertices, indices, faces: int, width: int, height: int, te
 
 
 def noise_error_stats(cfg, coords):
+    """FP32 against FP64 noise over every voxel of the chunks: (max abs error, voxels within
+    that error of the solid threshold, voxels whose solid bit differs)."""
     c = coords_array(coords)
     err = ctypes.c_double()
     near = ctypes.c_int64()

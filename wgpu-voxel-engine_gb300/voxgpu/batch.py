@@ -88,6 +88,7 @@ class BatchRun:
         return o0, o1
 
     def close(self):
+        """Destroys the captured graph and drops the output buffers."""
         if self.graph is not None:
             self.graph.close()
             self.graph = None
